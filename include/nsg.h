@@ -1,0 +1,160 @@
+/*
+ * nsg.h — C ABI of the GB300 sweep kernels for NetworkSolvers.jl.
+ *
+ * Every numerical step under the reference's plugin functions is reached through
+ * these entry points; the Julia (or Python) side keeps the drivers, region plans and
+ * problem types and holds opaque device handles.  Plain C types only; no exceptions
+ * cross this boundary; every call returns an `NSG_*` status and `nsg_last_error`
+ * gives the message.  All work is ordered on the context's CUDA stream; calls that
+ * return scalars (eigenvalue, kept bond dimension, truncation error, norms)
+ * synchronise that stream before returning.
+ *
+ * Layout contract: a tensor of rank r with dims (d0, ..., d{r-1}) is dense and
+ * column-major (d0 fastest) — the memory layout of an ITensor whose indices are in
+ * that order.  State tensors arrive with the index order fixed by
+ * permute_indices.jl:4-18 ([first link, site(s), other links]).
+ *
+ * Indices are named by int32 labels chosen by the caller (ITensor index ids with
+ * prime levels map to distinct labels).  Labels shared by two tensors are summed.
+ *
+ * Reference interfaces replaced (paths within emstoudenmire/NetworkSolvers.jl):
+ *   optimal_map(P::ProjTTN, ψ)          operator_map.jl:3-10   -> nsg_linmap_*, nsg_contract
+ *   ProjTTN environment update          extracter.jl:14        -> nsg_contract
+ *   local_state = prod(ψ[v] for region) extracter.jl:7         -> nsg_contract
+ *   eigsolve_solver (KrylovKit Lanczos) local_solvers/eigsolve.jl:3-29  -> nsg_eigsolve
+ *   exponentiate_solver (KrylovKit)     local_solvers/exponentiate.jl:3-29 -> nsg_exponentiate
+ *   runge_kutta_solver                  local_solvers/runge_kutta.jl:16-25 -> nsg_runge_kutta
+ *   it.factorize(local, indsTe; trunc)  inserter.jl:23         -> nsg_factorize
+ *   qr (gauge walk / 1-site TDVP)       extracter.jl:6, applyexp.jl:37 -> nsg_qr
+ *   eigen(rho; trunc, ishermitian)      subspace/densitymatrix.jl:53 -> nsg_eigh
+ *   directsum(A=>a, U=>u)               subspace/densitymatrix.jl:64 -> nsg_concat
+ *   norm / normalize / (T - P*T)        inserter.jl:31, densitymatrix.jl:48-59 -> nsg_norm, nsg_axpby, nsg_dot
+ */
+#ifndef NSG_H
+#define NSG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------- */
+#define NSG_OK 0
+#define NSG_ERR_INVALID 1        /* bad argument, shape or label set        */
+#define NSG_ERR_OOM 2            /* allocation beyond the context's budget  */
+#define NSG_ERR_CUDA 3           /* CUDA runtime error                      */
+#define NSG_ERR_NONFINITE 4      /* NaN/Inf in a scalar result              */
+#define NSG_ERR_NOT_CONVERGED 5  /* iteration limit reached                 */
+#define NSG_ERR_TIMEOUT 6        /* a bounded device-side wait gave up      */
+#define NSG_ERR_UNSUPPORTED 7
+
+/* ---- element types and precision modes ---------------------------------- */
+#define NSG_F64 0                /* real double                             */
+#define NSG_C128 1               /* complex double (re, im interleaved)     */
+
+#define NSG_PREC_FP64 0          /* every contraction in FP64               */
+#define NSG_PREC_TF32X3 1        /* large contractions: 3 TF32 products, FP32 accumulate */
+#define NSG_PREC_BF16X3 2        /* large contractions: 3 BF16 products, FP32 accumulate */
+#define NSG_PREC_BF16X6 3        /* large contractions: 6 BF16 products, FP32 accumulate */
+
+#define NSG_MAX_RANK 16
+
+typedef struct nsg_ctx nsg_ctx;
+typedef struct nsg_tensor nsg_tensor;
+typedef struct nsg_linmap nsg_linmap;
+
+/* ---- context --------------------------------------------------------------
+ * One context per host thread; it owns a CUDA stream, a stream-ordered device
+ * memory pool capped at `hbm_budget_bytes` (0 = no cap) and scratch buffers. */
+int nsg_ctx_create(int device, uint64_t hbm_budget_bytes, nsg_ctx** out);
+int nsg_ctx_destroy(nsg_ctx* ctx);
+const char* nsg_last_error(const nsg_ctx* ctx);
+int nsg_ctx_set_precision(nsg_ctx* ctx, int precision);
+int nsg_ctx_synchronize(nsg_ctx* ctx);
+/* bytes in use / peak / budget */
+int nsg_ctx_memory(const nsg_ctx* ctx, uint64_t* in_use, uint64_t* peak, uint64_t* budget);
+/* counters[0] = kernel launches, [1] = algorithmic flops of contractions,
+ * [2] = contraction calls, [3] = linear-map applications; reset if `reset`. */
+int nsg_ctx_counters(nsg_ctx* ctx, uint64_t* counters4, int reset);
+
+/* ---- tensors ------------------------------------------------------------- */
+int nsg_tensor_create(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims, nsg_tensor** out);
+int nsg_tensor_upload(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims,
+                      const void* host, nsg_tensor** out);
+int nsg_tensor_download(nsg_ctx* ctx, const nsg_tensor* t, void* host);
+int nsg_tensor_release(nsg_ctx* ctx, nsg_tensor* t);
+int nsg_tensor_shape(const nsg_tensor* t, int* dtype, int* rank, int64_t* dims);
+int nsg_tensor_copy(nsg_ctx* ctx, const nsg_tensor* src, nsg_tensor** out);
+/* device pointer (for callers that share device memory, e.g. torch) */
+int nsg_tensor_device_ptr(const nsg_tensor* t, void** ptr);
+
+/* ---- vector algebra on equally shaped tensors ---------------------------- */
+/* y = a*x + b*y (complex scalars given as re/im pairs; ignored im for F64) */
+int nsg_axpby(nsg_ctx* ctx, double a_re, double a_im, const nsg_tensor* x,
+              double b_re, double b_im, nsg_tensor* y);
+/* <x, y> = sum conj(x) y */
+int nsg_dot(nsg_ctx* ctx, const nsg_tensor* x, const nsg_tensor* y, double* re, double* im);
+int nsg_norm(nsg_ctx* ctx, const nsg_tensor* x, double* out);
+/* permute axes: out axis k = in axis perm[k]; optional complex conjugation */
+int nsg_permute(nsg_ctx* ctx, const nsg_tensor* x, const int* perm, int conj, nsg_tensor** out);
+/* concatenate along `axis` (all other dims equal)  — ITensors directsum */
+int nsg_concat(nsg_ctx* ctx, const nsg_tensor* a, const nsg_tensor* b, int axis, nsg_tensor** out);
+
+/* ---- contraction ---------------------------------------------------------
+ * Contract n tensors; tensor k has rank r_k (its own rank) and labels
+ * labels[off_k .. off_k + r_k) with off_k = sum of earlier ranks; conj[k] != 0
+ * conjugates tensor k.  Labels appearing twice are summed; the result has
+ * `out_rank` axes with labels `out_labels` (each appearing exactly once among the
+ * inputs).  The pairwise order minimises flops (exhaustive over subsets). */
+int nsg_contract(nsg_ctx* ctx, int n, nsg_tensor* const* tensors, const int32_t* labels,
+                 const int* conj, int out_rank, const int32_t* out_labels, nsg_tensor** out);
+
+/* A linear map y = M x built from fixed tensors and one vector slot (H_eff of
+ * optimal_map).  x has labels x_labels (x_rank of them); the result's axis k is the
+ * label y_labels[k] and is stored in x's shape (noprime).  Fixed-only parts of the
+ * contraction order are evaluated once at creation. */
+int nsg_linmap_create(nsg_ctx* ctx, int n_fixed, nsg_tensor* const* fixed,
+                      const int32_t* labels, const int* conj, int x_rank,
+                      const int32_t* x_labels, const int32_t* y_labels, nsg_linmap** out);
+int nsg_linmap_apply(nsg_ctx* ctx, nsg_linmap* m, const nsg_tensor* x, nsg_tensor* y);
+int nsg_linmap_release(nsg_ctx* ctx, nsg_linmap* m);
+/* flops of one application (algorithmic, real flops; complex MAC = 8) */
+int nsg_linmap_flops(const nsg_linmap* m, double* flops);
+
+/* ---- local solvers ------------------------------------------------------- */
+/* Lowest eigenpair (Lanczos, full reorthogonalisation).  x: initial vector in,
+ * normalised Ritz vector out. */
+int nsg_eigsolve(nsg_ctx* ctx, nsg_linmap* m, nsg_tensor* x, int krylovdim, int maxiter,
+                 double tol, double* eigval, int* numops);
+/* x <- exp(t M) x for Hermitian M, t complex (Lanczos exponential integrator). */
+int nsg_exponentiate(nsg_ctx* ctx, nsg_linmap* m, double t_re, double t_im, nsg_tensor* x,
+                     int krylovdim, int maxiter, double tol, int* converged, int* numops);
+/* x <- RK2/RK4 step of dx/dt = M x over t (runge_kutta.jl:2-14 algebra). */
+int nsg_runge_kutta(nsg_ctx* ctx, nsg_linmap* m, double t_re, double t_im, nsg_tensor* x,
+                    int order);
+
+/* ---- factorizations -------------------------------------------------------
+ * Matrix view: rows = axes left_axes[0..n_left) of T (in that order), columns = the
+ * remaining axes in storage order.  Singular values / eigenvalues are truncated by
+ * the NDTensors rule (relative discarded weight `cutoff`, `maxdim`, `mindim`;
+ * maxdim <= 0 means unlimited).  U: [left dims..., k], C: [k, right dims...]. */
+int nsg_factorize(nsg_ctx* ctx, const nsg_tensor* T, const int* left_axes, int n_left,
+                  double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
+                  nsg_tensor** C, int64_t* newdim, double* truncerr, double* spectrum,
+                  int64_t spectrum_cap);
+/* Q: [left dims..., k], R: [k, right dims...], k = min(rows, cols). */
+int nsg_qr(nsg_ctx* ctx, const nsg_tensor* T, const int* left_axes, int n_left,
+           nsg_tensor** Q, nsg_tensor** R);
+/* Hermitian eigen of rho viewed as (rows = axes row_axes) x (remaining axes), which
+ * must be the same space; eigenvalues descending, truncated.  U: [col dims..., k]
+ * (eigenvectors on the column space, the unprimed kets), evals: first k values. */
+int nsg_eigh(nsg_ctx* ctx, const nsg_tensor* rho, const int* row_axes, int n_row,
+             double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
+             double* evals, int64_t evals_cap, int64_t* newdim, double* truncerr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NSG_H */

@@ -1,0 +1,19 @@
+"""GB300-native sweep kernels for NetworkSolvers.jl (DMRG / TDVP region steps).
+
+Public API (same names as NetworkSolvers.jl): `dmrg`/`eigsolve`, `tdvp`/`applyexp`,
+the plugins `extracter`, `updater_eigsolve`, `updater_applyexp`, `inserter`,
+`subspace_expand`, the local solvers `eigsolve_solver`, `exponentiate_solver`,
+`runge_kutta_solver`, and the region plans.  The numerics run in libnsg.so
+(include/nsg.h); `build()` compiles it for sm_103a.
+"""
+from . import models
+from .build import build as build_library
+from .sweep import (dmrg, eigsolve, tdvp, applyexp, extracter, inserter, subspace_expand,
+                    updater_eigsolve, updater_applyexp, eigsolve_solver, exponentiate_solver,
+                    runge_kutta_solver, truncation_parameters, sweep_solve, region_iterator_action,
+                    EigsolveProblem, ApplyExpProblem)
+from .network import (euler_tour_edges, euler_tour_vertices, euler_sweep, post_order_dfs_plan,
+                      tdvp_regions, tdvp_sub_time_steps, TTN, ProjTTN, LinearMap, inner)
+from ._native import Context, default_context, set_default_context, NsgError
+
+__all__ = [n for n in dir() if not n.startswith("_")]

@@ -1,0 +1,156 @@
+"""ctypes binding of libnsg.so (the C ABI declared in include/nsg.h).
+
+The product path has no fallback: if the library is missing or no CUDA device is
+usable, `lib()` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_LIB = None
+
+OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_NONFINITE, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_UNSUPPORTED = range(8)
+F64, C128 = 0, 1
+PREC_FP64, PREC_TF32X3, PREC_BF16X3, PREC_BF16X6 = 0, 1, 2, 3
+PRECISIONS = {"fp64": PREC_FP64, "tf32x3": PREC_TF32X3, "bf16x3": PREC_BF16X3, "bf16x6": PREC_BF16X6}
+
+
+class NsgError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"nsg error {code}: {msg}")
+        self.code = code
+
+
+p = C.c_void_p
+i32 = C.c_int
+i64 = C.c_int64
+u64 = C.c_uint64
+dbl = C.c_double
+P_i64 = C.POINTER(C.c_int64)
+P_i32 = C.POINTER(C.c_int32)
+P_int = C.POINTER(C.c_int)
+P_dbl = C.POINTER(C.c_double)
+P_p = C.POINTER(C.c_void_p)
+
+_SIGS = {
+    "nsg_ctx_create": (i32, [i32, u64, P_p]),
+    "nsg_ctx_destroy": (i32, [p]),
+    "nsg_last_error": (C.c_char_p, [p]),
+    "nsg_ctx_set_precision": (i32, [p, i32]),
+    "nsg_ctx_synchronize": (i32, [p]),
+    "nsg_ctx_memory": (i32, [p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+    "nsg_ctx_counters": (i32, [p, C.POINTER(u64), i32]),
+    "nsg_tensor_create": (i32, [p, i32, i32, P_i64, P_p]),
+    "nsg_tensor_upload": (i32, [p, i32, i32, P_i64, p, P_p]),
+    "nsg_tensor_download": (i32, [p, p, p]),
+    "nsg_tensor_release": (i32, [p, p]),
+    "nsg_tensor_shape": (i32, [p, P_int, P_int, P_i64]),
+    "nsg_tensor_copy": (i32, [p, p, P_p]),
+    "nsg_tensor_device_ptr": (i32, [p, P_p]),
+    "nsg_axpby": (i32, [p, dbl, dbl, p, dbl, dbl, p]),
+    "nsg_dot": (i32, [p, p, p, P_dbl, P_dbl]),
+    "nsg_norm": (i32, [p, p, P_dbl]),
+    "nsg_permute": (i32, [p, p, P_int, i32, P_p]),
+    "nsg_concat": (i32, [p, p, p, i32, P_p]),
+    "nsg_contract": (i32, [p, i32, P_p, P_i32, P_int, i32, P_i32, P_p]),
+    "nsg_linmap_create": (i32, [p, i32, P_p, P_i32, P_int, i32, P_i32, P_i32, P_p]),
+    "nsg_linmap_apply": (i32, [p, p, p, p]),
+    "nsg_linmap_release": (i32, [p, p]),
+    "nsg_linmap_flops": (i32, [p, P_dbl]),
+    "nsg_eigsolve": (i32, [p, p, p, i32, i32, dbl, P_dbl, P_int]),
+    "nsg_exponentiate": (i32, [p, p, dbl, dbl, p, i32, i32, dbl, P_int, P_int]),
+    "nsg_runge_kutta": (i32, [p, p, dbl, dbl, p, i32]),
+    "nsg_factorize": (i32, [p, p, P_int, i32, dbl, i64, i64, P_p, P_p, P_i64, P_dbl, P_dbl, i64]),
+    "nsg_qr": (i32, [p, p, P_int, i32, P_p, P_p]),
+    "nsg_eigh": (i32, [p, p, P_int, i32, dbl, i64, i64, P_p, P_dbl, i64, P_i64, P_dbl]),
+}
+
+
+def lib_path() -> Path:
+    return Path(os.environ.get("NSG_LIB", Path(__file__).resolve().parent / "libnsg.so"))
+
+
+def lib():
+    """Load libnsg.so; raises if it was not built."""
+    global _LIB
+    if _LIB is None:
+        path = lib_path()
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: build it with `python -m networksolvers_gb300.build`")
+        L = C.CDLL(str(path))
+        for name, (res, args) in _SIGS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _LIB = L
+    return _LIB
+
+
+def exported_symbols():
+    return list(_SIGS)
+
+
+class Context:
+    """Owns an nsg_ctx (one CUDA stream + memory pool on one device)."""
+
+    def __init__(self, device=0, hbm_budget=0, precision="fp64"):
+        self.L = lib()
+        h = C.c_void_p()
+        self._check_raw(self.L.nsg_ctx_create(device, hbm_budget, C.byref(h)), None)
+        self.h = h
+        self.set_precision(precision)
+
+    def _check_raw(self, rc, h):
+        if rc != OK:
+            msg = self.L.nsg_last_error(h).decode() if h else "context creation failed"
+            raise NsgError(rc, msg)
+
+    def check(self, rc):
+        if rc != OK:
+            raise NsgError(rc, self.L.nsg_last_error(self.h).decode())
+
+    def set_precision(self, precision):
+        code = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.check(self.L.nsg_ctx_set_precision(self.h, code))
+        self.precision = precision
+
+    def synchronize(self):
+        self.check(self.L.nsg_ctx_synchronize(self.h))
+
+    def memory(self):
+        a, b, c = u64(), u64(), u64()
+        self.check(self.L.nsg_ctx_memory(self.h, C.byref(a), C.byref(b), C.byref(c)))
+        return a.value, b.value, c.value
+
+    def counters(self, reset=False):
+        arr = (u64 * 4)()
+        self.check(self.L.nsg_ctx_counters(self.h, arr, int(reset)))
+        return {"launches": arr[0], "flops": arr[1], "contractions": arr[2], "applies": arr[3]}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.nsg_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = None
+
+
+def default_context():
+    global _default
+    if _default is None:
+        _default = Context()
+    return _default
+
+
+def set_default_context(ctx):
+    global _default
+    _default = ctx

@@ -1,0 +1,271 @@
+// Context, device memory pool, tensor handles and the vector-algebra entry points.
+#include "nsg_internal.h"
+
+#include <cstring>
+#include <cmath>
+
+namespace nsg {
+
+void check_launch(const char* what) {
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) throw Error(NSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void* dalloc(nsg_ctx* c, size_t bytes) {
+  if (bytes == 0) bytes = 16;
+  bytes = (bytes + 255) & ~size_t(255);
+  if (c->budget && c->in_use + bytes > c->budget)
+    throw Error(NSG_ERR_OOM, "allocation of " + std::to_string(bytes) + " bytes exceeds the HBM budget (" +
+                                 std::to_string(c->in_use) + " of " + std::to_string(c->budget) + " in use)");
+  void* p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, c->stream);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw Error(NSG_ERR_OOM, std::string("cudaMallocAsync: ") + cudaGetErrorString(e));
+  }
+  c->in_use += bytes;
+  if (c->in_use > c->peak) c->peak = c->in_use;
+  return p;
+}
+
+void dfree(nsg_ctx* c, void* p, size_t bytes) {
+  if (!p) return;
+  if (bytes == 0) bytes = 16;
+  bytes = (bytes + 255) & ~size_t(255);
+  NSG_CUDA(cudaFreeAsync(p, c->stream));
+  c->in_use -= bytes;
+}
+
+nsg_tensor* new_tensor(nsg_ctx* c, int dtype, int rank, const int64_t* dims, bool zero) {
+  NSG_CHECK(dtype == NSG_F64 || dtype == NSG_C128, NSG_ERR_INVALID, "unknown dtype");
+  NSG_CHECK(rank >= 0 && rank <= NSG_MAX_RANK, NSG_ERR_INVALID, "rank out of range");
+  auto* t = new nsg_tensor();
+  t->dtype = dtype;
+  t->rank = rank;
+  t->size = 1;
+  for (int k = 0; k < rank; ++k) {
+    NSG_CHECK(dims[k] >= 1, NSG_ERR_INVALID, "tensor dimensions must be >= 1");
+    t->dims[k] = dims[k];
+    t->size *= dims[k];
+  }
+  t->bytes = size_t(t->size) * elem_bytes(dtype);
+  try {
+    t->data = dalloc(c, t->bytes);
+  } catch (...) {
+    delete t;
+    throw;
+  }
+  if (zero) NSG_CUDA(cudaMemsetAsync(t->data, 0, t->bytes, c->stream));
+  return t;
+}
+
+void free_tensor(nsg_ctx* c, nsg_tensor* t) {
+  if (!t) return;
+  dfree(c, t->data, t->bytes);
+  delete t;
+}
+
+double* host_scalars(nsg_ctx* c, size_t n) {
+  if (n > c->host_scalars_cap) {
+    if (c->host_scalars) cudaFreeHost(c->host_scalars);
+    size_t cap = n < 4096 ? 4096 : n;
+    NSG_CUDA(cudaMallocHost(&c->host_scalars, cap * sizeof(double)));
+    c->host_scalars_cap = cap;
+  }
+  return c->host_scalars;
+}
+
+double* dev_scratch(nsg_ctx* c, size_t n) {
+  if (n > c->dev_scratch_cap) {
+    if (c->dev_scratch) {
+      NSG_CUDA(cudaStreamSynchronize(c->stream));
+      NSG_CUDA(cudaFree(c->dev_scratch));
+    }
+    size_t cap = n < (1 << 16) ? (1 << 16) : n;
+    NSG_CUDA(cudaMalloc(&c->dev_scratch, cap * sizeof(double)));
+    c->dev_scratch_cap = cap;
+  }
+  return c->dev_scratch;
+}
+
+}  // namespace nsg
+
+using namespace nsg;
+
+extern "C" {
+
+int nsg_ctx_create(int device, uint64_t hbm_budget_bytes, nsg_ctx** out) {
+  nsg_ctx* c = nullptr;
+  NSG_API_BEGIN(c)
+  NSG_CHECK(out != nullptr, NSG_ERR_INVALID, "out is null");
+  int ndev = 0;
+  NSG_CUDA(cudaGetDeviceCount(&ndev));
+  NSG_CHECK(device >= 0 && device < ndev, NSG_ERR_INVALID, "no such CUDA device");
+  NSG_CUDA(cudaSetDevice(device));
+  c = new nsg_ctx();
+  c->device = device;
+  c->budget = hbm_budget_bytes;
+  NSG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  cudaMemPool_t pool;
+  NSG_CUDA(cudaDeviceGetDefaultMemPool(&pool, device));
+  uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+  NSG_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr));
+  NSG_CUDA(cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device));
+  *out = c;
+  c = nullptr;
+  NSG_API_END(c)
+}
+
+int nsg_ctx_destroy(nsg_ctx* c) {
+  if (!c) return NSG_OK;
+  cudaSetDevice(c->device);
+  cudaStreamSynchronize(c->stream);
+  if (c->host_scalars) cudaFreeHost(c->host_scalars);
+  if (c->dev_scratch) cudaFree(c->dev_scratch);
+  cudaStreamDestroy(c->stream);
+  delete c;
+  return NSG_OK;
+}
+
+const char* nsg_last_error(const nsg_ctx* c) { return c ? c->err.c_str() : "null context"; }
+
+int nsg_ctx_set_precision(nsg_ctx* c, int precision) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(precision >= NSG_PREC_FP64 && precision <= NSG_PREC_BF16X6, NSG_ERR_INVALID,
+            "unknown precision mode");
+  c->precision = precision;
+  NSG_API_END(c)
+}
+
+int nsg_ctx_synchronize(nsg_ctx* c) {
+  NSG_API_BEGIN(c)
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  NSG_API_END(c)
+}
+
+int nsg_ctx_memory(const nsg_ctx* c, uint64_t* in_use, uint64_t* peak, uint64_t* budget) {
+  if (!c) return NSG_ERR_INVALID;
+  if (in_use) *in_use = c->in_use;
+  if (peak) *peak = c->peak;
+  if (budget) *budget = c->budget;
+  return NSG_OK;
+}
+
+int nsg_ctx_counters(nsg_ctx* c, uint64_t* out, int reset) {
+  if (!c) return NSG_ERR_INVALID;
+  if (out) {
+    out[0] = c->launches;
+    out[1] = c->flops;
+    out[2] = c->contractions;
+    out[3] = c->applies;
+  }
+  if (reset) c->launches = c->flops = c->contractions = c->applies = 0;
+  return NSG_OK;
+}
+
+int nsg_tensor_create(nsg_ctx* c, int dtype, int rank, const int64_t* dims, nsg_tensor** out) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && out, NSG_ERR_INVALID, "null argument");
+  *out = new_tensor(c, dtype, rank, dims, true);
+  NSG_API_END(c)
+}
+
+int nsg_tensor_upload(nsg_ctx* c, int dtype, int rank, const int64_t* dims, const void* host,
+                      nsg_tensor** out) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && out && host, NSG_ERR_INVALID, "null argument");
+  nsg_tensor* t = new_tensor(c, dtype, rank, dims, false);
+  cudaError_t e = cudaMemcpyAsync(t->data, host, t->bytes, cudaMemcpyHostToDevice, c->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+  if (e != cudaSuccess) {
+    free_tensor(c, t);
+    throw Error(NSG_ERR_CUDA, std::string("upload: ") + cudaGetErrorString(e));
+  }
+  *out = t;
+  NSG_API_END(c)
+}
+
+int nsg_tensor_download(nsg_ctx* c, const nsg_tensor* t, void* host) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && t && host, NSG_ERR_INVALID, "null argument");
+  NSG_CUDA(cudaMemcpyAsync(host, t->data, t->bytes, cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  NSG_API_END(c)
+}
+
+int nsg_tensor_release(nsg_ctx* c, nsg_tensor* t) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c, NSG_ERR_INVALID, "null context");
+  free_tensor(c, t);
+  NSG_API_END(c)
+}
+
+int nsg_tensor_shape(const nsg_tensor* t, int* dtype, int* rank, int64_t* dims) {
+  if (!t) return NSG_ERR_INVALID;
+  if (dtype) *dtype = t->dtype;
+  if (rank) *rank = t->rank;
+  if (dims)
+    for (int k = 0; k < t->rank; ++k) dims[k] = t->dims[k];
+  return NSG_OK;
+}
+
+int nsg_tensor_device_ptr(const nsg_tensor* t, void** ptr) {
+  if (!t || !ptr) return NSG_ERR_INVALID;
+  *ptr = t->data;
+  return NSG_OK;
+}
+
+int nsg_tensor_copy(nsg_ctx* c, const nsg_tensor* src, nsg_tensor** out) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && src && out, NSG_ERR_INVALID, "null argument");
+  nsg_tensor* t = new_tensor(c, src->dtype, src->rank, src->dims, false);
+  NSG_CUDA(cudaMemcpyAsync(t->data, src->data, t->bytes, cudaMemcpyDeviceToDevice, c->stream));
+  *out = t;
+  NSG_API_END(c)
+}
+
+int nsg_axpby(nsg_ctx* c, double ar, double ai, const nsg_tensor* x, double br, double bi,
+              nsg_tensor* y) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && x && y, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(x->dtype == y->dtype && x->size == y->size, NSG_ERR_INVALID, "axpby: shape/dtype mismatch");
+  axpby(c, x->dtype, x->size, ar, ai, x->data, br, bi, y->data);
+  NSG_API_END(c)
+}
+
+int nsg_dot(nsg_ctx* c, const nsg_tensor* x, const nsg_tensor* y, double* re, double* im) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && x && y, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(x->dtype == y->dtype && x->size == y->size, NSG_ERR_INVALID, "dot: shape/dtype mismatch");
+  double out[2] = {0, 0};
+  const void* v[1] = {x->data};
+  multi_dot(c, x->dtype, x->size, 1, v, y->data, out);
+  if (re) *re = out[0];
+  if (im) *im = x->dtype == NSG_C128 ? out[1] : 0.0;
+  NSG_API_END(c)
+}
+
+int nsg_norm(nsg_ctx* c, const nsg_tensor* x, double* out) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && x && out, NSG_ERR_INVALID, "null argument");
+  *out = norm2(c, x->dtype, x->size, x->data);
+  NSG_API_END(c)
+}
+
+int nsg_permute(nsg_ctx* c, const nsg_tensor* x, const int* perm, int conj, nsg_tensor** out) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && x && out, NSG_ERR_INVALID, "null argument");
+  int64_t dims[NSG_MAX_RANK];
+  std::vector<int> seen(x->rank, 0);
+  for (int k = 0; k < x->rank; ++k) {
+    NSG_CHECK(perm[k] >= 0 && perm[k] < x->rank && !seen[perm[k]], NSG_ERR_INVALID, "bad permutation");
+    seen[perm[k]] = 1;
+    dims[k] = x->dims[perm[k]];
+  }
+  nsg_tensor* t = new_tensor(c, x->dtype, x->rank, dims, false);
+  permute(c, x, perm, conj != 0, t);
+  *out = t;
+  NSG_API_END(c)
+}
+
+}  // extern "C"

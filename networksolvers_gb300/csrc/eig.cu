@@ -1,0 +1,425 @@
+// Truncated factorizations of the inserter and the subspace expansion:
+//   it.factorize(local, indsTe; cutoff, maxdim, mindim)   inserter.jl:23
+//   qr(...)                                               extracter.jl:6, applyexp.jl:37
+//   eigen(rho; trunc..., ishermitian=true)                 subspace/densitymatrix.jl:53
+//
+// The SVD of the matricised tensor M (m x n) goes through the Hermitian Gram matrix
+// G = M M^H: G = Z diag(lambda) Z^H gives the left singular vectors U = Z and
+// sigma^2 = lambda, and C = U^H M = S V^H is the right factor that `factorize` with
+// ortho="left" stores (U -> psi[v1], C -> psi[v2]).  The eigensolver is a parallel
+// cyclic Jacobi method (round-robin pairing, n/2 disjoint rotations per round,
+// complex Hermitian rotations for complex128).  Its orthogonality is at the unit
+// roundoff regardless of eigenvalue clustering, which the spectra of DMRG bonds
+// (exact SU(2) multiplets, long tails) need.
+//
+// Truncation rule (NDTensors, restated): spectrum P = lambda sorted descending,
+// negative tail zeroed; cut to maxdim; then drop from the end while
+// (discarded + P[n] < cutoff * sum(P)) and n > mindim.
+#include "nsg_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+
+namespace nsg {
+
+namespace {
+
+constexpr int kJacobiThreads = 1024;
+constexpr int kJacobiMaxN = 2048;
+
+__device__ __forceinline__ double re_(double v) { return v; }
+__device__ __forceinline__ double re_(double2 v) { return v.x; }
+__device__ __forceinline__ double abs_(double v) { return fabs(v); }
+__device__ __forceinline__ double abs_(double2 v) { return hypot(v.x, v.y); }
+
+// rotate a pair (x_p, x_q) with J = [[c, s], [-s e, c e]] where e = conj(phase) (columns)
+// For real data phase = 1.
+__device__ __forceinline__ void rot_cols(double& xp, double& xq, double c, double s, double2) {
+  double a = xp, b = xq;
+  xp = c * a - s * b;
+  xq = s * a + c * b;
+}
+__device__ __forceinline__ void rot_cols(double2& xp, double2& xq, double c, double s, double2 e) {
+  // col_p' = c col_p - s e col_q ; col_q' = s col_p + c e col_q   with e = exp(-i phi)
+  double2 a = xp, b = xq;
+  double2 eb = make_double2(e.x * b.x - e.y * b.y, e.x * b.y + e.y * b.x);
+  xp = make_double2(c * a.x - s * eb.x, c * a.y - s * eb.y);
+  xq = make_double2(s * a.x + c * eb.x, s * a.y + c * eb.y);
+}
+__device__ __forceinline__ void rot_rows(double& xp, double& xq, double c, double s, double2) {
+  double a = xp, b = xq;
+  xp = c * a - s * b;
+  xq = s * a + c * b;
+}
+__device__ __forceinline__ void rot_rows(double2& xp, double2& xq, double c, double s, double2 e) {
+  // rows <- J^H rows: row_p' = c row_p - s conj(e) row_q ; row_q' = s row_p + c conj(e) row_q
+  double2 a = xp, b = xq;
+  double2 ce = make_double2(e.x, -e.y);
+  double2 eb = make_double2(ce.x * b.x - ce.y * b.y, ce.x * b.y + ce.y * b.x);
+  xp = make_double2(c * a.x - s * eb.x, c * a.y - s * eb.y);
+  xq = make_double2(s * a.x + c * eb.x, s * a.y + c * eb.y);
+}
+__device__ __forceinline__ double2 phase_of(double b) { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ double2 phase_of(double2 b) {
+  double r = hypot(b.x, b.y);
+  return r > 0 ? make_double2(b.x / r, -b.y / r) : make_double2(1.0, 0.0);  // exp(-i phi)
+}
+__device__ __forceinline__ void set_one(double& v) { v = 1.0; }
+__device__ __forceinline__ void set_one(double2& v) { v = make_double2(1.0, 0.0); }
+__device__ __forceinline__ void set_zero(double& v) { v = 0.0; }
+__device__ __forceinline__ void set_zero(double2& v) { v = make_double2(0.0, 0.0); }
+
+// One CTA diagonalises G (n x n, column-major, Hermitian, overwritten) and writes V.
+// Round-robin schedule over N = n rounded up to even players: in round r, player N-1
+// meets r, and (r+i) mod (N-1) meets (r-i) mod (N-1) for i = 1..N/2-1.
+template <typename T>
+__global__ void __launch_bounds__(kJacobiThreads)
+    jacobi_kernel(T* __restrict__ G, int n, T* __restrict__ V, double* __restrict__ w, int max_sweeps,
+                  int* __restrict__ sweeps_out) {
+  __shared__ double cs_[kJacobiMaxN / 2], sn_[kJacobiMaxN / 2];
+  __shared__ double2 ph_[kJacobiMaxN / 2];
+  __shared__ int p_[kJacobiMaxN / 2], q_[kJacobiMaxN / 2];
+  __shared__ int any_rot;
+  __shared__ double red[kJacobiThreads / 32];
+  __shared__ double scale;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int64_t nn = int64_t(n) * n;
+  for (int64_t e = tid; e < nn; e += nt) {
+    int64_t i = e % n, j = e / n;
+    if (i == j)
+      set_one(V[e]);
+    else
+      set_zero(V[e]);
+  }
+  // Frobenius norm of G for the absolute threshold
+  double loc = 0.0;
+  for (int64_t e = tid; e < nn; e += nt) {
+    double a = abs_(G[e]);
+    loc += a * a;
+  }
+  for (int o = 16; o > 0; o >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, o);
+  if ((tid & 31) == 0) red[tid >> 5] = loc;
+  __syncthreads();
+  if (tid == 0) {
+    double s = 0;
+    for (int k = 0; k < (nt + 31) / 32; ++k) s += red[k];
+    scale = sqrt(s);
+  }
+  __syncthreads();
+  const double abs_thr = 1e-17 * scale;
+  const int N = n + (n & 1);
+  const int npairs = N / 2;
+  int sweep = 0;
+  for (; sweep < max_sweeps; ++sweep) {
+    if (tid == 0) any_rot = 0;
+    __syncthreads();
+    for (int r = 0; r < N - 1; ++r) {
+      for (int k = tid; k < npairs; k += nt) {
+        int p, q;
+        if (k == 0) {
+          p = N - 1;
+          q = r;
+        } else {
+          p = (r + k) % (N - 1);
+          q = (r - k + (N - 1)) % (N - 1);
+        }
+        if (p > q) {
+          int t = p;
+          p = q;
+          q = t;
+        }
+        double c = 1.0, s = 0.0;
+        double2 e = make_double2(1.0, 0.0);
+        if (q < n) {
+          double a = re_(G[p + int64_t(n) * p]), d = re_(G[q + int64_t(n) * q]);
+          T b = G[p + int64_t(n) * q];
+          double bb = abs_(b);
+          if (bb > abs_thr && bb > 1e-16 * sqrt(fabs(a) * fabs(d))) {
+            double theta = (d - a) / (2.0 * bb);
+            double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            c = 1.0 / sqrt(t * t + 1.0);
+            s = t * c;
+            e = phase_of(b);
+            any_rot = 1;
+          }
+        }
+        p_[k] = p;
+        q_[k] = (q < n) ? q : -1;
+        cs_[k] = c;
+        sn_[k] = s;
+        ph_[k] = e;
+      }
+      __syncthreads();
+      // columns of G and V
+      const int64_t tasks = int64_t(npairs) * n;
+      for (int64_t t = tid; t < tasks; t += nt) {
+        int k = int(t / n), i = int(t % n);
+        int q = q_[k];
+        if (q < 0 || sn_[k] == 0.0) continue;
+        int p = p_[k];
+        rot_cols(G[i + int64_t(n) * p], G[i + int64_t(n) * q], cs_[k], sn_[k], ph_[k]);
+        rot_cols(V[i + int64_t(n) * p], V[i + int64_t(n) * q], cs_[k], sn_[k], ph_[k]);
+      }
+      __syncthreads();
+      // rows of G
+      for (int64_t t = tid; t < tasks; t += nt) {
+        int k = int(t / n), j = int(t % n);
+        int q = q_[k];
+        if (q < 0 || sn_[k] == 0.0) continue;
+        int p = p_[k];
+        rot_rows(G[p + int64_t(n) * j], G[q + int64_t(n) * j], cs_[k], sn_[k], ph_[k]);
+      }
+      __syncthreads();
+    }
+    if (!any_rot) break;
+    __syncthreads();
+  }
+  for (int i = tid; i < n; i += nt) w[i] = re_(G[i + int64_t(n) * i]);
+  if (tid == 0 && sweeps_out) *sweeps_out = sweep;
+}
+
+struct Spectrum {
+  std::vector<int> order;  // indices sorted by descending eigenvalue
+  std::vector<double> P;   // sorted, negative tail zeroed
+};
+
+Spectrum sorted_spectrum(const std::vector<double>& w) {
+  Spectrum s;
+  s.order.resize(w.size());
+  std::iota(s.order.begin(), s.order.end(), 0);
+  std::stable_sort(s.order.begin(), s.order.end(), [&](int a, int b) { return w[a] > w[b]; });
+  for (int i : s.order) s.P.push_back(w[i]);
+  return s;
+}
+
+// NDTensors truncation rule; returns kept count and relative discarded weight.
+int64_t truncate_rule(std::vector<double> P, int64_t origm, double cutoff, int64_t maxdim, int64_t mindim,
+                      double* truncerr) {
+  P.resize(origm);
+  for (int64_t n = origm - 1; n >= 0; --n) {
+    if (P[n] >= 0) break;
+    P[n] = 0.0;
+  }
+  int64_t md = (maxdim <= 0) ? origm : std::min<int64_t>(maxdim, origm);
+  int64_t n = origm;
+  double err = 0.0;
+  while (n > md) {
+    err += P[n - 1];
+    --n;
+  }
+  double scale = 0.0;
+  for (double x : P) scale += x;
+  if (scale == 0.0) scale = 1.0;
+  while (n > mindim && err + P[n - 1] < cutoff * scale) {
+    err += P[n - 1];
+    --n;
+  }
+  if (n < 1) n = 1;
+  *truncerr = err / scale;
+  return n;
+}
+
+// permute T so that the listed axes come first; returns matrix dims
+nsg_tensor* matricize(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, int64_t* m, int64_t* ncol,
+                      std::vector<int64_t>& ldims, std::vector<int64_t>& rdims, bool* owned) {
+  std::vector<int> perm;
+  std::vector<int> used(T->rank, 0);
+  for (int k = 0; k < n_left; ++k) {
+    NSG_CHECK(left_axes[k] >= 0 && left_axes[k] < T->rank && !used[left_axes[k]], NSG_ERR_INVALID,
+              "factorize: bad left axes");
+    used[left_axes[k]] = 1;
+    perm.push_back(left_axes[k]);
+  }
+  for (int k = 0; k < T->rank; ++k)
+    if (!used[k]) perm.push_back(k);
+  *m = 1;
+  *ncol = 1;
+  ldims.clear();
+  rdims.clear();
+  for (int k = 0; k < T->rank; ++k) {
+    int64_t d = T->dims[perm[k]];
+    if (k < n_left) {
+      *m *= d;
+      ldims.push_back(d);
+    } else {
+      *ncol *= d;
+      rdims.push_back(d);
+    }
+  }
+  bool ident = true;
+  for (int k = 0; k < T->rank; ++k) ident &= perm[k] == k;
+  if (ident) {
+    *owned = false;
+    return const_cast<nsg_tensor*>(T);
+  }
+  int64_t dims[NSG_MAX_RANK];
+  for (int k = 0; k < T->rank; ++k) dims[k] = T->dims[perm[k]];
+  nsg_tensor* P = new_tensor(c, T->dtype, T->rank, dims, false);
+  permute(c, T, perm.data(), false, P);
+  *owned = true;
+  return P;
+}
+
+}  // namespace
+
+void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev) {
+  NSG_CHECK(n >= 1 && n <= kJacobiMaxN, NSG_ERR_UNSUPPORTED,
+            "eigensolver: matrix order " + std::to_string(n) + " above the supported maximum");
+  int threads = kJacobiThreads;
+  if (dtype == NSG_C128)
+    jacobi_kernel<double2><<<1, threads, 0, c->stream>>>((double2*)A, int(n), (double2*)V, w_dev, 60, nullptr);
+  else
+    jacobi_kernel<double><<<1, threads, 0, c->stream>>>((double*)A, int(n), (double*)V, w_dev, 60, nullptr);
+  count_launch(c);
+  check_launch("jacobi");
+}
+
+// Hermitian eigendecomposition of an m x m matrix stored in `Mat` (column-major,
+// consumed): returns sorted spectrum and the eigenvector matrix Z (device).
+static void gram_eig(nsg_ctx* c, int dtype, int64_t m, void* Mat, void* Z, Spectrum& sp) {
+  double* wdev = (double*)dalloc(c, sizeof(double) * m);
+  syevd(c, dtype, m, Mat, Z, wdev);
+  std::vector<double> w(m);
+  NSG_CUDA(cudaMemcpyAsync(w.data(), wdev, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  dfree(c, wdev, sizeof(double) * m);
+  for (double x : w) NSG_CHECK(std::isfinite(x), NSG_ERR_NONFINITE, "eigensolver: non-finite eigenvalue");
+  sp = sorted_spectrum(w);
+}
+
+}  // namespace nsg
+
+using namespace nsg;
+
+static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, double cutoff,
+                          int64_t maxdim, int64_t mindim, nsg_tensor** U, nsg_tensor** C, int64_t* newdim,
+                          double* truncerr, double* spectrum, int64_t spectrum_cap) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && T && U && C, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(n_left >= 1 && n_left < T->rank, NSG_ERR_INVALID, "factorize: need left and right axes");
+  int64_t m, ncol;
+  std::vector<int64_t> ldims, rdims;
+  bool owned = false;
+  nsg_tensor* M = matricize(c, T, left_axes, n_left, &m, &ncol, ldims, rdims, &owned);
+  const int dt = T->dtype;
+  const size_t eb = elem_bytes(dt);
+  // G = M M^H
+  void* G = dalloc(c, eb * m * m);
+  GemmArgs g;
+  g.dtype = dt;
+  g.M = m;
+  g.N = m;
+  g.K = ncol;
+  g.A = M->data;
+  g.lda = m;
+  g.opA = OP_N;
+  g.B = M->data;
+  g.ldb = m;
+  g.opB = OP_C;
+  g.C = G;
+  g.ldc = m;
+  g.batch = 1;
+  g.strideA = g.strideB = g.strideC = 0;
+  gemm_f64_simt(c, g);  // the Gram matrix and its eigenvectors stay FP64 in every precision mode
+  void* Z = dalloc(c, eb * m * m);
+  Spectrum sp;
+  gram_eig(c, dt, m, G, Z, sp);
+  dfree(c, G, eb * m * m);
+  int64_t origm = std::min(m, ncol);
+  double err = 0.0;
+  int64_t k = truncate_rule(sp.P, origm, cutoff, maxdim, mindim, &err);
+  // U = Z[:, order[0..k)]
+  std::vector<int64_t> udims = ldims;
+  udims.push_back(k);
+  nsg_tensor* Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+  int* didx = (int*)dalloc(c, sizeof(int) * k);
+  NSG_CUDA(cudaMemcpyAsync(didx, sp.order.data(), sizeof(int) * k, cudaMemcpyHostToDevice, c->stream));
+  copy_columns(c, dt, m, k, Z, m, didx, Ut->data, m);
+  dfree(c, didx, sizeof(int) * k);
+  dfree(c, Z, eb * m * m);
+  // C = U^H M
+  std::vector<int64_t> cdims;
+  cdims.push_back(k);
+  for (auto d : rdims) cdims.push_back(d);
+  nsg_tensor* Ct = new_tensor(c, dt, int(cdims.size()), cdims.data(), false);
+  GemmArgs h;
+  h.dtype = dt;
+  h.M = k;
+  h.N = ncol;
+  h.K = m;
+  h.A = Ut->data;
+  h.lda = m;
+  h.opA = OP_C;
+  h.B = M->data;
+  h.ldb = m;
+  h.opB = OP_N;
+  h.C = Ct->data;
+  h.ldc = k;
+  h.batch = 1;
+  h.strideA = h.strideB = h.strideC = 0;
+  gemm_f64_simt(c, h);
+  if (owned) free_tensor(c, M);
+  if (spectrum)
+    for (int64_t i = 0; i < std::min<int64_t>(spectrum_cap, origm); ++i)
+      spectrum[i] = i < int64_t(sp.P.size()) ? std::max(sp.P[i], 0.0) : 0.0;
+  *U = Ut;
+  *C = Ct;
+  if (newdim) *newdim = k;
+  if (truncerr) *truncerr = err;
+  NSG_API_END(c)
+}
+
+extern "C" {
+
+int nsg_factorize(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, double cutoff, int64_t maxdim,
+                  int64_t mindim, nsg_tensor** U, nsg_tensor** C, int64_t* newdim, double* truncerr,
+                  double* spectrum, int64_t spectrum_cap) {
+  return factorize_impl(c, T, left_axes, n_left, cutoff, maxdim, mindim, U, C, newdim, truncerr, spectrum,
+                        spectrum_cap);
+}
+
+int nsg_qr(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, nsg_tensor** Q, nsg_tensor** R) {
+  int64_t k;
+  double err;
+  return factorize_impl(c, T, left_axes, n_left, 0.0, 0, 1, Q, R, &k, &err, nullptr, 0);
+}
+
+int nsg_eigh(nsg_ctx* c, const nsg_tensor* rho, const int* row_axes, int n_row, double cutoff, int64_t maxdim,
+             int64_t mindim, nsg_tensor** U, double* evals, int64_t evals_cap, int64_t* newdim, double* truncerr) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && rho && U, NSG_ERR_INVALID, "null argument");
+  int64_t m, ncol;
+  std::vector<int64_t> ldims, rdims;
+  bool owned = false;
+  nsg_tensor* M = matricize(c, rho, row_axes, n_row, &m, &ncol, ldims, rdims, &owned);
+  NSG_CHECK(m == ncol, NSG_ERR_INVALID, "eigh: row and column spaces differ in size");
+  const int dt = rho->dtype;
+  const size_t eb = elem_bytes(dt);
+  void* A = dalloc(c, eb * m * m);
+  NSG_CUDA(cudaMemcpyAsync(A, M->data, eb * m * m, cudaMemcpyDeviceToDevice, c->stream));
+  if (owned) free_tensor(c, M);
+  void* Z = dalloc(c, eb * m * m);
+  Spectrum sp;
+  gram_eig(c, dt, m, A, Z, sp);
+  dfree(c, A, eb * m * m);
+  double err = 0.0;
+  int64_t k = truncate_rule(sp.P, m, cutoff, maxdim, mindim, &err);
+  std::vector<int64_t> udims = rdims;
+  udims.push_back(k);
+  nsg_tensor* Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+  int* didx = (int*)dalloc(c, sizeof(int) * k);
+  NSG_CUDA(cudaMemcpyAsync(didx, sp.order.data(), sizeof(int) * k, cudaMemcpyHostToDevice, c->stream));
+  copy_columns(c, dt, m, k, Z, m, didx, Ut->data, m);
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  dfree(c, didx, sizeof(int) * k);
+  dfree(c, Z, eb * m * m);
+  if (evals)
+    for (int64_t i = 0; i < std::min(evals_cap, k); ++i) evals[i] = sp.P[i];
+  *U = Ut;
+  if (newdim) *newdim = k;
+  if (truncerr) *truncerr = err;
+  NSG_API_END(c)
+}
+
+}  // extern "C"

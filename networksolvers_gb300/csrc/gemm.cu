@@ -1,0 +1,172 @@
+// FP64 / complex-FP64 strided-batched GEMM on the CUDA cores (the plain form).
+//
+// C_b = alpha * op(A_b) * op(B_b) + beta * C_b, column-major, op in {N, T, C, R}.
+// GB300 executes FP64 at a small fraction of its FP32 rate, so this kernel is
+// compute-bound for every shape that matters; a 64x64 tile with 4x4 outputs per
+// thread keeps the FP64 pipes busy.  Loads are mapped so that consecutive threads
+// touch consecutive addresses for either operand orientation.
+#include "nsg_internal.h"
+
+namespace nsg {
+
+namespace {
+
+constexpr int BM = 64, BN = 64, NT = 256;
+
+__device__ __forceinline__ double ld(const double* p, bool) { return *p; }
+__device__ __forceinline__ double2 ld(const double2* p, bool conj) {
+  double2 v = *p;
+  if (conj) v.y = -v.y;
+  return v;
+}
+__device__ __forceinline__ void zero(double& v) { v = 0.0; }
+__device__ __forceinline__ void zero(double2& v) { v = make_double2(0.0, 0.0); }
+__device__ __forceinline__ void mac(double& acc, double a, double b) { acc = fma(a, b, acc); }
+__device__ __forceinline__ void mac(double2& acc, double2 a, double2 b) {
+  acc.x = fma(a.x, b.x, fma(-a.y, b.y, acc.x));
+  acc.y = fma(a.x, b.y, fma(a.y, b.x, acc.y));
+}
+
+template <typename T>
+struct Scal;
+template <>
+struct Scal<double> {
+  double a, b;
+  __device__ double epi(double acc, const double* c) const { return b == 0.0 ? a * acc : fma(a, acc, b * (*c)); }
+};
+template <>
+struct Scal<double2> {
+  double2 a, b;
+  __device__ double2 epi(double2 acc, const double2* c) const {
+    double2 r = make_double2(a.x * acc.x - a.y * acc.y, a.x * acc.y + a.y * acc.x);
+    if (b.x != 0.0 || b.y != 0.0) {
+      double2 cv = *c;
+      r.x += b.x * cv.x - b.y * cv.y;
+      r.y += b.x * cv.y + b.y * cv.x;
+    }
+    return r;
+  }
+};
+
+template <typename T, int BK>
+__global__ void __launch_bounds__(NT)
+    gemm_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_t lda, int64_t sA, int opA,
+                const T* __restrict__ B, int64_t ldb, int64_t sB, int opB, T* __restrict__ C, int64_t ldc,
+                int64_t sC, int64_t batch, Scal<T> sc) {
+  __shared__ T As[BK][BM + 1];
+  __shared__ T Bs[BK][BN + 1];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int64_t m0 = int64_t(blockIdx.x) * BM, n0 = int64_t(blockIdx.y) * BN;
+  const bool transA = (opA == OP_T || opA == OP_C), conjA = (opA == OP_C || opA == OP_R);
+  const bool transB = (opB == OP_T || opB == OP_C), conjB = (opB == OP_C || opB == OP_R);
+  for (int64_t bz = blockIdx.z; bz < batch; bz += gridDim.z) {
+    const T* Ab = A + bz * sA;
+    const T* Bb = B + bz * sB;
+    T* Cb = C + bz * sC;
+    T acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) zero(acc[i][j]);
+    for (int64_t k0 = 0; k0 < K; k0 += BK) {
+      // A tile: BM x BK
+#pragma unroll
+      for (int r = 0; r < (BM * BK) / NT; ++r) {
+        int e = threadIdx.x + r * NT;
+        int i, k;
+        if (!transA) {
+          i = e % BM;
+          k = e / BM;
+        } else {
+          k = e % BK;
+          i = e / BK;
+        }
+        int64_t gi = m0 + i, gk = k0 + k;
+        T v;
+        zero(v);
+        if (gi < M && gk < K) v = ld(transA ? Ab + gk + gi * lda : Ab + gi + gk * lda, conjA);
+        As[k][i] = v;
+      }
+      // B tile: BK x BN
+#pragma unroll
+      for (int r = 0; r < (BN * BK) / NT; ++r) {
+        int e = threadIdx.x + r * NT;
+        int j, k;
+        if (!transB) {
+          k = e % BK;
+          j = e / BK;
+        } else {
+          j = e % BN;
+          k = e / BN;
+        }
+        int64_t gj = n0 + j, gk = k0 + k;
+        T v;
+        zero(v);
+        if (gj < N && gk < K) v = ld(transB ? Bb + gj + gk * ldb : Bb + gk + gj * ldb, conjB);
+        Bs[k][j] = v;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int k = 0; k < BK; ++k) {
+        T a[4], b[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = As[k][ty + 16 * i];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) b[j] = Bs[k][tx + 16 * j];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) mac(acc[i][j], a[i], b[j]);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      int64_t gi = m0 + ty + 16 * i;
+      if (gi >= M) continue;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        int64_t gj = n0 + tx + 16 * j;
+        if (gj >= N) continue;
+        T* cp = Cb + gi + gj * ldc;
+        *cp = sc.epi(acc[i][j], cp);
+      }
+    }
+  }
+}
+
+}  // namespace
+
+void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
+  if (g.M == 0 || g.N == 0 || g.batch == 0) return;
+  int64_t gx = (g.M + BM - 1) / BM, gy = (g.N + BN - 1) / BN;
+  NSG_CHECK(gx < (1ll << 31) && gy < 65536, NSG_ERR_UNSUPPORTED, "gemm: grid too large");
+  int64_t gz = g.batch < 65535 ? g.batch : 65535;
+  dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
+  if (g.dtype == NSG_C128) {
+    Scal<double2> sc{make_double2(g.alpha_re, g.alpha_im), make_double2(g.beta_re, g.beta_im)};
+    gemm_kernel<double2, 8><<<grid, NT, 0, c->stream>>>(g.M, g.N, g.K, (const double2*)g.A, g.lda, g.strideA, g.opA,
+                                                        (const double2*)g.B, g.ldb, g.strideB, g.opB,
+                                                        (double2*)g.C, g.ldc, g.strideC, g.batch, sc);
+  } else {
+    Scal<double> sc{g.alpha_re, g.beta_re};
+    gemm_kernel<double, 16><<<grid, NT, 0, c->stream>>>(g.M, g.N, g.K, (const double*)g.A, g.lda, g.strideA, g.opA,
+                                                        (const double*)g.B, g.ldb, g.strideB, g.opB, (double*)g.C,
+                                                        g.ldc, g.strideC, g.batch, sc);
+  }
+  count_launch(c);
+  check_launch("gemm_f64_simt");
+}
+
+void gemm(nsg_ctx* c, const GemmArgs& g) {
+  double mac = double(g.M) * double(g.N) * double(g.K) * double(g.batch);
+  c->flops += uint64_t(mac * (g.dtype == NSG_C128 ? 8.0 : 2.0));
+  if (g.K == 0) {
+    // C = beta*C (alpha term vanishes)
+    return;
+  }
+  if (c->precision != NSG_PREC_FP64 && gemm_split_tc(c, g)) return;
+  gemm_f64_simt(c, g);
+}
+
+}  // namespace nsg

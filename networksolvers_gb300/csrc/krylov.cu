@@ -1,0 +1,303 @@
+// Local solvers of local_solvers/*.jl, with every Krylov vector resident on the
+// device.  Only the scalars of the recurrence (alpha, beta, projection
+// coefficients) come back to the host, where the k x k tridiagonal problems
+// (k <= krylovdim) are solved in FP64.
+//
+//  * nsg_eigsolve      — KrylovKit `eigsolve(..., :SR; krylovdim, maxiter, tol)` as
+//                        called by local_solvers/eigsolve.jl:16-27 (Lanczos).
+//  * nsg_exponentiate  — KrylovKit `exponentiate(A, t, x; krylovdim, tol, maxiter,
+//                        eager)`, local_solvers/exponentiate.jl:16-27.
+//  * nsg_runge_kutta   — runge_kutta.jl:2-25.
+//
+// Lanczos step (shared by both Krylov solvers): w = A v_j - beta_{j-1} v_{j-1},
+// then two full classical Gram-Schmidt passes against v_0..v_j; alpha_j is the sum
+// of the two projections on v_j and beta_j = ||w||.
+#include "nsg_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+
+namespace nsg {
+void linmap_apply(nsg_ctx* c, nsg_linmap* m, const nsg_tensor* x, nsg_tensor* y);
+
+// Dense symmetric eigensolver for small host matrices (cyclic Jacobi).
+// A: n x n column-major (destroyed), w: eigenvalues ascending, V: eigenvectors.
+static void sym_eig_small(int n, std::vector<double>& A, std::vector<double>& w, std::vector<double>& V) {
+  V.assign(size_t(n) * n, 0.0);
+  for (int i = 0; i < n; ++i) V[i + size_t(n) * i] = 1.0;
+  auto a = [&](int i, int j) -> double& { return A[i + size_t(n) * j]; };
+  for (int sweep = 0; sweep < 100; ++sweep) {
+    double off = 0, tot = 0;
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < n; ++i) {
+        tot += a(i, j) * a(i, j);
+        if (i != j) off += a(i, j) * a(i, j);
+      }
+    if (off <= 1e-34 * tot || off == 0.0) break;
+    for (int p = 0; p < n - 1; ++p)
+      for (int q = p + 1; q < n; ++q) {
+        double apq = a(p, q);
+        if (std::fabs(apq) < 1e-300) continue;
+        double theta = (a(q, q) - a(p, p)) / (2 * apq);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1));
+        double cs = 1 / std::sqrt(t * t + 1), sn = t * cs;
+        for (int k = 0; k < n; ++k) {  // columns
+          double akp = a(k, p), akq = a(k, q);
+          a(k, p) = cs * akp - sn * akq;
+          a(k, q) = sn * akp + cs * akq;
+        }
+        for (int k = 0; k < n; ++k) {  // rows
+          double apk = a(p, k), aqk = a(q, k);
+          a(p, k) = cs * apk - sn * aqk;
+          a(q, k) = sn * apk + cs * aqk;
+        }
+        for (int k = 0; k < n; ++k) {
+          double vkp = V[k + size_t(n) * p], vkq = V[k + size_t(n) * q];
+          V[k + size_t(n) * p] = cs * vkp - sn * vkq;
+          V[k + size_t(n) * q] = sn * vkp + cs * vkq;
+        }
+      }
+  }
+  std::vector<int> idx(n);
+  for (int i = 0; i < n; ++i) idx[i] = i;
+  std::sort(idx.begin(), idx.end(), [&](int x, int y) { return a(x, x) < a(y, y); });
+  std::vector<double> Vs(size_t(n) * n);
+  w.resize(n);
+  for (int k = 0; k < n; ++k) {
+    w[k] = a(idx[k], idx[k]);
+    for (int i = 0; i < n; ++i) Vs[i + size_t(n) * k] = V[i + size_t(n) * idx[k]];
+  }
+  V.swap(Vs);
+}
+
+void tridiag_eig(int n, const double* alpha, const double* beta, double* evals, double* evecs) {
+  std::vector<double> A(size_t(n) * n, 0.0), w, V;
+  for (int i = 0; i < n; ++i) {
+    A[i + size_t(n) * i] = alpha[i];
+    if (i + 1 < n) A[i + size_t(n) * (i + 1)] = A[(i + 1) + size_t(n) * i] = beta[i];
+  }
+  sym_eig_small(n, A, w, V);
+  for (int i = 0; i < n; ++i) evals[i] = w[i];
+  for (size_t i = 0; i < size_t(n) * n; ++i) evecs[i] = V[i];
+}
+
+namespace {
+
+struct Vecs {
+  nsg_ctx* c;
+  std::vector<nsg_tensor*> v;
+  explicit Vecs(nsg_ctx* cc) : c(cc) {}
+  ~Vecs() {
+    for (auto* t : v) free_tensor(c, t);
+  }
+  nsg_tensor* add(const nsg_tensor* like) {
+    v.push_back(new_tensor(c, like->dtype, like->rank, like->dims, false));
+    return v.back();
+  }
+};
+
+// One Lanczos expansion: given V[0..j] (orthonormal), computes w, alpha_j, beta_j.
+void lanczos_step(nsg_ctx* c, nsg_linmap* m, std::vector<nsg_tensor*>& V, int j, nsg_tensor* w,
+                  const std::vector<double>& beta, double* alpha_j, double* beta_j) {
+  const int dt = w->dtype;
+  const int64_t n = w->size;
+  linmap_apply(c, m, V[j], w);
+  if (j > 0) axpby(c, dt, n, -beta[j - 1], 0.0, V[j - 1]->data, 1.0, 0.0, w->data);
+  std::vector<const void*> ptrs(j + 1);
+  for (int i = 0; i <= j; ++i) ptrs[i] = V[i]->data;
+  std::vector<double> co(2 * (j + 1)), neg(2 * (j + 1));
+  double a = 0.0;
+  for (int pass = 0; pass < 2; ++pass) {
+    multi_dot(c, dt, n, j + 1, ptrs.data(), w->data, co.data());
+    for (int i = 0; i < 2 * (j + 1); ++i) neg[i] = -co[i];
+    multi_axpy(c, dt, n, j + 1, ptrs.data(), neg.data(), w->data);
+    a += co[2 * j];
+  }
+  double b = norm2(c, dt, n, w->data);
+  if (!std::isfinite(a) || !std::isfinite(b)) throw Error(NSG_ERR_NONFINITE, "Lanczos: non-finite scalar");
+  *alpha_j = a;
+  *beta_j = b;
+}
+
+}  // namespace
+}  // namespace nsg
+
+using namespace nsg;
+
+extern "C" {
+
+int nsg_eigsolve(nsg_ctx* c, nsg_linmap* m, nsg_tensor* x, int krylovdim, int maxiter, double tol, double* eigval,
+                 int* numops) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && m && x && eigval, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(krylovdim >= 1 && krylovdim <= 64 && maxiter >= 1, NSG_ERR_INVALID, "eigsolve: krylovdim 1..64");
+  const int dt = x->dtype;
+  const int64_t n = x->size;
+  Vecs store(c);
+  std::vector<nsg_tensor*> V;
+  for (int i = 0; i < krylovdim; ++i) V.push_back(store.add(x));
+  nsg_tensor* w = store.add(x);
+  int ops = 0;
+  double lam = 0.0;
+  double nx = norm2(c, dt, n, x->data);
+  NSG_CHECK(nx > 0 && std::isfinite(nx), NSG_ERR_NONFINITE, "eigsolve: zero or non-finite start vector");
+  axpby(c, dt, n, 1.0 / nx, 0.0, x->data, 0.0, 0.0, V[0]->data);
+  for (int it = 0; it < maxiter; ++it) {
+    std::vector<double> alpha, beta;
+    int k = 0;
+    for (int j = 0; j < krylovdim; ++j) {
+      double a, b;
+      beta.resize(j + 1);
+      lanczos_step(c, m, V, j, w, beta, &a, &b);
+      ++ops;
+      alpha.push_back(a);
+      beta[j] = b;
+      k = j + 1;
+      if (j + 1 == krylovdim || b <= tol) break;
+      axpby(c, dt, n, 1.0 / b, 0.0, w->data, 0.0, 0.0, V[j + 1]->data);
+    }
+    std::vector<double> ev(k), Y(size_t(k) * k);
+    tridiag_eig(k, alpha.data(), beta.data(), ev.data(), Y.data());
+    lam = ev[0];
+    std::vector<double> coef(2 * k, 0.0);
+    for (int j = 0; j < k; ++j) coef[2 * j] = Y[j];
+    std::vector<const void*> ptrs(k);
+    for (int j = 0; j < k; ++j) ptrs[j] = V[j]->data;
+    NSG_CUDA(cudaMemsetAsync(x->data, 0, x->bytes, c->stream));
+    multi_axpy(c, dt, n, k, ptrs.data(), coef.data(), x->data);
+    double nr = norm2(c, dt, n, x->data);
+    axpby(c, dt, n, 1.0 / nr, 0.0, x->data, 0.0, 0.0, x->data);
+    if (std::fabs(beta[k - 1] * Y[k - 1]) <= tol || it + 1 == maxiter) break;
+    NSG_CUDA(cudaMemcpyAsync(V[0]->data, x->data, x->bytes, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  *eigval = lam;
+  if (numops) *numops = ops;
+  NSG_API_END(c)
+}
+
+int nsg_exponentiate(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_tensor* x, int krylovdim,
+                     int maxiter, double tol, int* converged, int* numops) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && m && x, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(krylovdim >= 1 && krylovdim <= 64 && maxiter >= 1, NSG_ERR_INVALID, "exponentiate: krylovdim 1..64");
+  NSG_CHECK(t_im == 0.0 || x->dtype == NSG_C128, NSG_ERR_INVALID, "exponentiate: complex time needs a complex vector");
+  const int dt = x->dtype;
+  const int64_t n = x->size;
+  using cd = std::complex<double>;
+  const cd t(t_re, t_im);
+  int ops = 0;
+  if (converged) *converged = 1;
+  if (std::abs(t) == 0.0) {
+    if (numops) *numops = 0;
+    return NSG_OK;
+  }
+  Vecs store(c);
+  std::vector<nsg_tensor*> V;
+  for (int i = 0; i < krylovdim; ++i) V.push_back(store.add(x));
+  nsg_tensor* w = store.add(x);
+  cd remaining = t;
+  bool done = false;
+  for (int it = 0; it < maxiter && !done; ++it) {
+    double beta0 = norm2(c, dt, n, x->data);
+    if (beta0 == 0.0) break;
+    NSG_CHECK(std::isfinite(beta0), NSG_ERR_NONFINITE, "exponentiate: non-finite vector");
+    axpby(c, dt, n, 1.0 / beta0, 0.0, x->data, 0.0, 0.0, V[0]->data);
+    std::vector<double> alpha, beta;
+    std::vector<cd> E;  // first column of exp(tau T_k)
+    double err = INFINITY;
+    int k = 0;
+    auto expm_col = [&](int kk, cd tau, std::vector<cd>& col) {
+      std::vector<double> ev(kk), Q(size_t(kk) * kk);
+      tridiag_eig(kk, alpha.data(), beta.data(), ev.data(), Q.data());
+      col.assign(kk, cd(0, 0));
+      for (int i = 0; i < kk; ++i)
+        for (int l = 0; l < kk; ++l) col[i] += Q[i + size_t(kk) * l] * std::exp(tau * ev[l]) * Q[0 + size_t(kk) * l];
+    };
+    for (int j = 0; j < krylovdim; ++j) {
+      double a, b;
+      beta.resize(j + 1);
+      lanczos_step(c, m, V, j, w, beta, &a, &b);
+      ++ops;
+      alpha.push_back(a);
+      beta[j] = b;
+      k = j + 1;
+      expm_col(k, remaining, E);
+      err = beta0 * b * std::abs(E[k - 1]);
+      if (err <= tol || b <= tol * 1e-3 || j + 1 == krylovdim) break;
+      axpby(c, dt, n, 1.0 / b, 0.0, w->data, 0.0, 0.0, V[j + 1]->data);
+    }
+    cd step = remaining;
+    if (!(err <= tol || beta[k - 1] <= tol * 1e-3)) {
+      double s = 0.5;
+      while (true) {
+        step = remaining * s;
+        expm_col(k, step, E);
+        double e2 = beta0 * beta[k - 1] * std::abs(E[k - 1]);
+        if (e2 <= tol * std::abs(step) / std::abs(t) || s < 1e-12) break;
+        s *= 0.5;
+      }
+    }
+    std::vector<double> coef(2 * k);
+    for (int j = 0; j < k; ++j) {
+      cd cj = beta0 * E[j];
+      coef[2 * j] = cj.real();
+      coef[2 * j + 1] = cj.imag();
+    }
+    std::vector<const void*> ptrs(k);
+    for (int j = 0; j < k; ++j) ptrs[j] = V[j]->data;
+    NSG_CUDA(cudaMemsetAsync(x->data, 0, x->bytes, c->stream));
+    multi_axpy(c, dt, n, k, ptrs.data(), coef.data(), x->data);
+    remaining -= step;
+    if (std::abs(remaining) <= 1e-15 * std::abs(t)) done = true;
+  }
+  if (converged) *converged = done ? 1 : 0;
+  if (numops) *numops = ops;
+  NSG_API_END(c)
+}
+
+int nsg_runge_kutta(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_tensor* x, int order) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && m && x, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(order == 2 || order == 4, NSG_ERR_INVALID, "For runge_kutta_solver, must specify `order` keyword");
+  NSG_CHECK(t_im == 0.0 || x->dtype == NSG_C128, NSG_ERR_INVALID, "runge_kutta: complex time needs a complex vector");
+  const int dt = x->dtype;
+  const int64_t n = x->size;
+  Vecs store(c);
+  nsg_tensor* k1 = store.add(x);
+  nsg_tensor* kb = store.add(x);
+  nsg_tensor* tmp = store.add(x);
+  std::complex<double> t(t_re, t_im);
+  if (order == 2) {
+    linmap_apply(c, m, x, k1);    // H psi
+    linmap_apply(c, m, k1, tmp);  // H^2 psi
+    std::complex<double> h2 = t * t / 2.0;
+    axpby(c, dt, n, t.real(), t.imag(), k1->data, 1.0, 0.0, x->data);
+    axpby(c, dt, n, h2.real(), h2.imag(), tmp->data, 1.0, 0.0, x->data);
+    return NSG_OK;
+  }
+  nsg_tensor* acc = store.add(x);
+  std::complex<double> h = t / 2.0, t6 = t / 6.0;
+  linmap_apply(c, m, x, k1);  // k1 = H psi
+  NSG_CUDA(cudaMemcpyAsync(acc->data, k1->data, x->bytes, cudaMemcpyDeviceToDevice, c->stream));
+  // k2 = k1 + (t/2) H k1
+  linmap_apply(c, m, k1, tmp);
+  NSG_CUDA(cudaMemcpyAsync(kb->data, k1->data, x->bytes, cudaMemcpyDeviceToDevice, c->stream));
+  axpby(c, dt, n, h.real(), h.imag(), tmp->data, 1.0, 0.0, kb->data);
+  axpby(c, dt, n, 2.0, 0.0, kb->data, 1.0, 0.0, acc->data);
+  // k3 = k1 + (t/2) H k2
+  linmap_apply(c, m, kb, tmp);
+  NSG_CUDA(cudaMemcpyAsync(kb->data, k1->data, x->bytes, cudaMemcpyDeviceToDevice, c->stream));
+  axpby(c, dt, n, h.real(), h.imag(), tmp->data, 1.0, 0.0, kb->data);
+  axpby(c, dt, n, 2.0, 0.0, kb->data, 1.0, 0.0, acc->data);
+  // k4 = k1 + t H k3
+  linmap_apply(c, m, kb, tmp);
+  NSG_CUDA(cudaMemcpyAsync(kb->data, k1->data, x->bytes, cudaMemcpyDeviceToDevice, c->stream));
+  axpby(c, dt, n, t.real(), t.imag(), tmp->data, 1.0, 0.0, kb->data);
+  axpby(c, dt, n, 1.0, 0.0, kb->data, 1.0, 0.0, acc->data);
+  // psi += (t/6) acc
+  axpby(c, dt, n, t6.real(), t6.imag(), acc->data, 1.0, 0.0, x->data);
+  NSG_API_END(c)
+}
+
+}  // extern "C"

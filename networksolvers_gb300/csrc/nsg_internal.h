@@ -1,0 +1,137 @@
+// Internal declarations shared by the nsg translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+#include <vector>
+#include <stdexcept>
+
+#include "../../include/nsg.h"
+
+namespace nsg {
+
+// ---------------------------------------------------------------------------
+// errors: internal code throws nsg::Error; every extern "C" entry point catches
+// and turns it into a status code plus the context's last-error message.
+// ---------------------------------------------------------------------------
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define NSG_CUDA(call)                                                              \
+  do {                                                                              \
+    cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess)                                                          \
+      throw ::nsg::Error(NSG_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+#define NSG_CHECK(cond, code, msg)                                                  \
+  do {                                                                              \
+    if (!(cond)) throw ::nsg::Error((code), (msg));                                 \
+  } while (0)
+
+struct Ctx;
+
+}  // namespace nsg
+
+struct nsg_tensor {
+  int dtype = NSG_F64;
+  int rank = 0;
+  int64_t dims[NSG_MAX_RANK] = {};
+  int64_t size = 1;  // number of elements
+  void* data = nullptr;
+  size_t bytes = 0;
+};
+
+struct nsg_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  uint64_t budget = 0, in_use = 0, peak = 0;
+  int precision = NSG_PREC_FP64;
+  std::string err;
+  uint64_t launches = 0, flops = 0, contractions = 0, applies = 0;
+  // pinned host staging for scalar readback
+  double* host_scalars = nullptr;
+  size_t host_scalars_cap = 0;
+  // device scratch for reductions
+  double* dev_scratch = nullptr;
+  size_t dev_scratch_cap = 0;
+  int num_sms = 0;
+};
+
+namespace nsg {
+
+inline size_t elem_bytes(int dtype) { return dtype == NSG_C128 ? 16 : 8; }
+
+// memory
+void* dalloc(nsg_ctx* c, size_t bytes);
+void dfree(nsg_ctx* c, void* p, size_t bytes);
+nsg_tensor* new_tensor(nsg_ctx* c, int dtype, int rank, const int64_t* dims, bool zero = false);
+void free_tensor(nsg_ctx* c, nsg_tensor* t);
+double* host_scalars(nsg_ctx* c, size_t n);
+double* dev_scratch(nsg_ctx* c, size_t n);
+inline void count_launch(nsg_ctx* c, int n = 1) { c->launches += n; }
+void check_launch(const char* what);
+
+// ---------------------------------------------------------------------------
+// kernels (launchers)
+// ---------------------------------------------------------------------------
+// op: 0 = N, 1 = T, 2 = C (conjugate transpose), 3 = R (conjugate, no transpose)
+enum Op { OP_N = 0, OP_T = 1, OP_C = 2, OP_R = 3 };
+
+struct GemmArgs {
+  int dtype;
+  int64_t M, N, K;
+  const void* A; int64_t lda; int64_t strideA; int opA;
+  const void* B; int64_t ldb; int64_t strideB; int opB;
+  void* C; int64_t ldc; int64_t strideC;
+  int64_t batch;
+  double alpha_re = 1.0, alpha_im = 0.0, beta_re = 0.0, beta_im = 0.0;
+};
+// dispatches by the context's precision mode and shape
+void gemm(nsg_ctx* c, const GemmArgs& g);
+void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g);
+bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g);  // false if not applicable
+
+void permute(nsg_ctx* c, const nsg_tensor* x, const int* perm, bool conj, nsg_tensor* out);
+void axpby(nsg_ctx* c, int dtype, int64_t n, double ar, double ai, const void* x, double br,
+           double bi, void* y);
+// out[j] = <v_j, w> for j < nv (complex: 2 doubles each), written to host buffer
+void multi_dot(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, const void* w,
+               double* host_out);
+// w += sum_j coef_j v_j (coef complex pairs)
+void multi_axpy(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v,
+                const double* coef, void* w);
+double norm2(nsg_ctx* c, int dtype, int64_t n, const void* x);
+void scale(nsg_ctx* c, int dtype, int64_t n, double ar, double ai, void* x);
+void copy_columns(nsg_ctx* c, int dtype, int64_t rows, int64_t ncols, const void* src,
+                  int64_t lds, const int* d_colidx, void* dst, int64_t ldd);
+void copy_rows(nsg_ctx* c, int dtype, int64_t nrows_out, int64_t ncols, const void* src,
+               int64_t lds, void* dst, int64_t ldd);
+void row_norms2(nsg_ctx* c, int dtype, int64_t rows, int64_t cols, const void* A, int64_t lda,
+                double* out_dev);
+// symmetric/Hermitian eigen of a dense n x n matrix (column-major, overwritten);
+// eigenvectors to V (n x n), eigenvalues (unsorted) to w_dev.
+void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev);
+
+// host helpers
+void tridiag_eig(int n, const double* alpha, const double* beta, double* evals, double* evecs);
+
+}  // namespace nsg
+
+// extern "C" guard helper
+#define NSG_API_BEGIN(ctx) try {
+#define NSG_API_END(ctx)                                                   \
+  }                                                                        \
+  catch (const ::nsg::Error& e) {                                          \
+    if (ctx) (ctx)->err = e.what();                                        \
+    return e.code;                                                         \
+  }                                                                        \
+  catch (const std::exception& e) {                                        \
+    if (ctx) (ctx)->err = e.what();                                        \
+    return NSG_ERR_INVALID;                                                \
+  }                                                                        \
+  return NSG_OK;

@@ -2,8 +2,9 @@
 
 * `eigsolve_lanczos` — KrylovKit `eigsolve(A, x0, 1, :SR; krylovdim, maxiter, tol,
   ishermitian=true)` as called by local_solvers/eigsolve.jl:16-27: Lanczos with full
-  reorthogonalisation (restated as classical Gram-Schmidt applied twice, which spans
-  the same Krylov space as KrylovKit's ModifiedGramSchmidtIR), Ritz pair of the
+  reorthogonalisation (restated as the three-term recurrence followed by two full
+  classical Gram-Schmidt passes; alpha is the sum of the two projections on the newest
+  vector.  This spans the same Krylov space as KrylovKit's ModifiedGramSchmidtIR), Ritz pair of the
   smallest Ritz value.  A factorisation of dimension k costs k operator applications.
   Restarts (maxiter > 1) restart from the Ritz vector; every workload here uses
   maxiter = 1, the reference default.
@@ -47,8 +48,7 @@ def lanczos_factorization(A, v0, kmax, breakdown, eager_check=None):
         # the projections onto the newest vector correct alpha
         if len(V) > 1:
             w = w - beta[-1] * V[-2]
-        a = _dot(V[-1], w)
-        w = w - a * V[-1]
+        a = 0.0
         for _pass in range(2):
             coeffs = [_dot(v, w) for v in V]
             for c, v in zip(coeffs, V):

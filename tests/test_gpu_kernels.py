@@ -1,0 +1,254 @@
+"""Kernel-level parity on the GPU, through the C ABI (libnsg.so via ctypes):
+contractions (every GEMM orientation, batched forms, conjugation, permutes),
+truncated factorisation, QR, Hermitian eigen, Lanczos, Krylov exponential and RK4,
+each against numpy / the oracle on the same seeded inputs.
+Tolerances: FP64 contractions 1e-12 relative; eigenvalues 1e-12 relative;
+truncated bond dimensions exact."""
+import numpy as np
+import pytest
+
+from networksolvers_gb300 import itensors as it
+from networksolvers_gb300.itensors import DTensor, Index, contract
+from oracle import krylov as ok, linalg as ol
+from oracle.tensor import Index as OIndex, Tensor as OTensor
+
+pytestmark = pytest.mark.gpu
+
+
+def rnd(rng, shape, cplx=False):
+    a = rng.standard_normal(shape)
+    if cplx:
+        a = a + 1j * rng.standard_normal(shape)
+    return a
+
+
+def rel(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_contract_layouts(nsg_ctx, cplx):
+    rng = np.random.default_rng(1)
+    i, j, k, l, m_ = (Index(d) for d in (7, 5, 6, 4, 3))
+    cases = [
+        ((i, k), (k, j)),          # N N
+        ((k, i), (k, j)),          # T N
+        ((i, k), (j, k)),          # N T
+        ((k, i), (j, k)),          # T T
+        ((i, k, l), (k, j)),       # A batched over l
+        ((i, k, l), (j, k)),
+        ((i, j), (m_, k, j, l)),   # B batched
+        ((k, l, i), (l, j, k)),    # K order mismatch -> permute
+        ((i, k, j, l), (l, k)),    # K interleaved -> permute
+        ((i,), (i, j)),            # vector
+    ]
+    for ia, ib in cases:
+        a = rnd(rng, [x.dim for x in ia], cplx)
+        b = rnd(rng, [x.dim for x in ib], cplx)
+        for conj_a in (False, True):
+            A = DTensor.from_numpy(a, ia)
+            B = DTensor.from_numpy(b, ib)
+            if conj_a:
+                A = A.dag()
+            Cd = A * B
+            aa = np.conj(a) if (conj_a and cplx) else a
+            lab = {}
+            for x in list(ia) + list(ib):
+                lab.setdefault(x, len(lab))
+            ref = np.einsum(aa, [lab[x] for x in ia], b, [lab[x] for x in ib], [lab[x] for x in Cd.inds])
+            assert rel(Cd.to_numpy(), ref) < 1e-12, (ia, ib, conj_a)
+
+
+def test_contract_network_and_output_order(nsg_ctx):
+    rng = np.random.default_rng(2)
+    chi, w, d = 9, 5, 2
+    a, ap, b, bp = Index(chi), Index(chi), Index(chi), Index(chi)
+    w1, w2, w3 = Index(w), Index(w), Index(w)
+    s1, s2 = Index(d), Index(d)
+    L = rnd(rng, (chi, w, chi)); R = rnd(rng, (chi, w, chi))
+    W1 = rnd(rng, (w, d, d, w)); W2 = rnd(rng, (w, d, d, w)); x = rnd(rng, (chi, d, d, chi))
+    t = [DTensor.from_numpy(L, [ap, w1, a]), DTensor.from_numpy(W1, [w1, s1.prime(), s1, w2]),
+         DTensor.from_numpy(W2, [w2, s2.prime(), s2, w3]), DTensor.from_numpy(R, [bp, w3, b]),
+         DTensor.from_numpy(x, [a, s1, s2, b])]
+    out = [ap, s1.prime(), s2.prime(), bp]
+    y = contract(t, out=out).to_numpy()
+    ref = np.einsum("pwa,wtsv,vuxz,qzb,asxb->ptuq", L, W1, W2, R, x)
+    assert rel(y, ref) < 1e-12
+
+
+@pytest.mark.parametrize("perm", [(1, 0, 2), (2, 0, 1), (0, 2, 1, 3), (3, 1, 0, 2), (1, 2, 0, 3)])
+def test_permute(nsg_ctx, perm):
+    rng = np.random.default_rng(3)
+    shape = [5, 33, 7, 40][: len(perm)]
+    a = rnd(rng, shape, True)
+    inds = [Index(s) for s in shape]
+    T = DTensor.from_numpy(a, inds)
+    P = T.permute([inds[p] for p in perm])
+    assert np.array_equal(P.to_numpy(), np.transpose(a, perm))
+    Pc = T.dag().permute([inds[p] for p in perm])
+    assert np.array_equal(Pc.to_numpy(), np.conj(np.transpose(a, perm)))
+
+
+def _spectrum_matrix(rng, m, n, decay, cplx):
+    k = min(m, n)
+    U, _ = np.linalg.qr(rnd(rng, (m, k), cplx))
+    V, _ = np.linalg.qr(rnd(rng, (n, k), cplx))
+    s = decay ** np.arange(k)
+    return (U * s) @ V.conj().T
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("m,n", [(16, 16), (24, 10), (10, 24), (128, 128)])
+def test_factorize_truncation(nsg_ctx, cplx, m, n):
+    rng = np.random.default_rng(m * 100 + n)
+    M = _spectrum_matrix(rng, m, n, 0.55, cplx)
+    l, r = Index(m), Index(n)
+    T = DTensor.from_numpy(M, [l, r])
+    for cutoff, maxdim in [(0.0, None), (1e-10, None), (1e-6, 8), (1e-3, None)]:
+        U, Cc, info = it.factorize(T, [l], cutoff=cutoff, maxdim=maxdim, spectrum=True)
+        s = np.linalg.svd(M, compute_uv=False)
+        kref, errref = ol.truncate_spectrum(s ** 2, cutoff, maxdim)
+        assert info["newdim"] == kref
+        assert abs(info["truncerr"] - errref) <= 1e-9 * max(errref, 1e-16) + 1e-15
+        u = U.to_numpy()
+        c = Cc.to_numpy()
+        assert np.allclose(u.conj().T @ u, np.eye(kref), atol=1e-12)
+        Pk = u @ c
+        s2 = s[:kref]
+        assert rel(np.linalg.svd(Pk, compute_uv=False)[:kref], s2) < 1e-10
+        assert abs(np.linalg.norm(M - Pk) ** 2 / np.linalg.norm(M) ** 2 - errref) < 1e-10
+
+
+def test_factorize_tensor_axes(nsg_ctx):
+    rng = np.random.default_rng(5)
+    a, s1, s2, b = Index(6), Index(2), Index(2), Index(5)
+    x = rnd(rng, (6, 2, 2, 5))
+    T = DTensor.from_numpy(x, [a, s1, s2, b])
+    U, Cc, info = it.factorize(T, [s1, a], cutoff=0.0)
+    recon = contract([U, Cc], out=[a, s1, s2, b]).to_numpy()
+    assert rel(recon, x) < 1e-12
+    Q, R = it.qr(T, [a, s1])
+    assert Q.inds[-1].dim == 10
+    assert rel(contract([Q, R], out=[a, s1, s2, b]).to_numpy(), x) < 1e-12
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_eigh_truncated(nsg_ctx, cplx):
+    rng = np.random.default_rng(6)
+    a0, s = Index(7), Index(2)
+    S = rnd(rng, (14, 9), cplx)
+    rho = (S @ S.conj().T).reshape(7, 2, 7, 2)
+    T = DTensor.from_numpy(rho, [a0.prime(), s.prime(), a0, s])
+    D, U, u = it.eigen_hermitian(T, [a0, s], cutoff=1e-8, maxdim=5)
+    w = np.sort(np.linalg.eigvalsh(S @ S.conj().T))[::-1]
+    kref, _ = ol.truncate_spectrum(w, 1e-8, 5)
+    assert len(D) == kref and rel(D, w[:kref]) < 1e-12
+    Um = U.to_numpy().reshape(14, kref)
+    M = S @ S.conj().T
+    assert rel(M @ Um, Um * D) < 1e-10
+
+
+def _chain_heff(rng, chi_l, chi_r, w=5, d=2, cplx=False):
+    """A Hermitian 2-site H_eff: L, W1, W2, R hermitised so that the map is Hermitian."""
+    def herm_env(chi):
+        E = rnd(rng, (chi, w, chi), cplx)
+        return E + np.conj(np.transpose(E, (2, 1, 0)))
+    def herm_op():
+        W = rnd(rng, (w, d, d, w), cplx)
+        return W + np.conj(np.transpose(W, (0, 2, 1, 3)))
+    return herm_env(chi_l), herm_op(), herm_op(), herm_env(chi_r)
+
+
+def _heff_numpy(L, W1, W2, R):
+    return lambda x: np.einsum("pwa,wtsv,vuxz,qzb,asxb->ptuq", L, W1, W2, R, x)
+
+
+def _device_map(L, W1, W2, R):
+    from networksolvers_gb300.network import LinearMap
+    chi_l, chi_r = L.shape[0], R.shape[0]
+    w, d = W1.shape[0], W1.shape[1]
+    a, b = Index(chi_l, "Link"), Index(chi_r, "Link")
+    w1, w2, w3 = Index(w), Index(w), Index(w)
+    s1, s2 = Index(d, "Site"), Index(d, "Site")
+
+    class P:
+        def map_tensors(self):
+            return [DTensor.from_numpy(L, [a.prime(), w1, a]), DTensor.from_numpy(W1, [w1, s1.prime(), s1, w2]),
+                    DTensor.from_numpy(W2, [w2, s2.prime(), s2, w3]), DTensor.from_numpy(R, [b.prime(), w3, b])]
+    return LinearMap(P(), [a, s1, s2, b]), [a, s1, s2, b]
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+def test_linmap_matches_numpy(nsg_ctx, cplx):
+    rng = np.random.default_rng(7)
+    L, W1, W2, R = _chain_heff(rng, 11, 13, cplx=cplx)
+    lm, inds = _device_map(L, W1, W2, R)
+    x = rnd(rng, (11, 2, 2, 13), cplx)
+    y = lm(DTensor.from_numpy(x, inds)).to_numpy()
+    assert rel(y, _heff_numpy(L, W1, W2, R)(x)) < 1e-12
+    assert lm.flops() > 0
+
+
+@pytest.mark.parametrize("krylovdim,maxiter", [(3, 1), (6, 3)])
+def test_lanczos_matches_oracle(nsg_ctx, krylovdim, maxiter):
+    from networksolvers_gb300.sweep import eigsolve_solver
+    rng = np.random.default_rng(8)
+    L, W1, W2, R = _chain_heff(rng, 12, 10)
+    lm, inds = _device_map(L, W1, W2, R)
+    x0 = rnd(rng, (12, 2, 2, 10))
+    lam, x = eigsolve_solver(lm, DTensor.from_numpy(x0, inds), krylovdim=krylovdim, maxiter=maxiter)
+    lam_o, x_o = ok.eigsolve_lanczos(_heff_numpy(L, W1, W2, R), x0, krylovdim=krylovdim, maxiter=maxiter)
+    assert abs(lam - lam_o) <= 1e-12 * abs(lam_o)
+    assert abs(abs(np.vdot(x.to_numpy(), x_o)) - 1) < 1e-12
+
+
+def test_lanczos_breakdown_small_space(nsg_ctx):
+    """Local space smaller than krylovdim (chain end): the factorisation stops on breakdown."""
+    from networksolvers_gb300.sweep import eigsolve_solver
+    rng = np.random.default_rng(9)
+    L, W1, W2, R = _chain_heff(rng, 1, 1)
+    lm, inds = _device_map(L, W1, W2, R)
+    x0 = rnd(rng, (1, 2, 2, 1))
+    lam, x = eigsolve_solver(lm, DTensor.from_numpy(x0, inds), krylovdim=8, maxiter=1)
+    H = _heff_numpy(L, W1, W2, R)
+    dense = np.stack([H(e.reshape(1, 2, 2, 1)).ravel() for e in np.eye(4)], axis=1)
+    assert abs(lam - np.linalg.eigvalsh(dense)[0]) < 1e-11
+
+
+def test_exponentiate_and_rk4(nsg_ctx):
+    from networksolvers_gb300.sweep import exponentiate_solver, runge_kutta_solver
+    import scipy.linalg as sla
+    rng = np.random.default_rng(10)
+    L, W1, W2, R = _chain_heff(rng, 5, 4, cplx=True)
+    lm, inds = _device_map(L, W1, W2, R)
+    H = _heff_numpy(L, W1, W2, R)
+    n = 5 * 2 * 2 * 4
+    dense = np.stack([H(e.reshape(5, 2, 2, 4)).ravel() for e in np.eye(n)], axis=1)
+    x0 = rnd(rng, (5, 2, 2, 4), True)
+    x0 /= np.linalg.norm(x0)
+    t = -0.05j
+    y, info = exponentiate_solver(lm, t, DTensor.from_numpy(x0, inds))
+    exact = (sla.expm(t * dense) @ x0.ravel()).reshape(x0.shape)
+    assert rel(y.to_numpy(), exact) < 1e-10
+    y_o, _ = ok.exponentiate(H, t, x0)
+    assert rel(y.to_numpy(), y_o) < 1e-11
+    z, _ = runge_kutta_solver(lm, t, DTensor.from_numpy(x0, inds), order=4)
+    assert rel(z.to_numpy(), ok.runge_kutta_4(H, t, x0)) < 1e-12
+    z2, _ = runge_kutta_solver(lm, t, DTensor.from_numpy(x0, inds), order=2)
+    assert rel(z2.to_numpy(), ok.runge_kutta_2(H, t, x0)) < 1e-12
+
+
+def test_concat_directsum(nsg_ctx):
+    rng = np.random.default_rng(11)
+    a0, s, a, u = Index(4), Index(2), Index(3), Index(2)
+    A = rnd(rng, (4, 2, 3)); U = rnd(rng, (4, 2, 2))
+    Ax, ax = it.directsum(DTensor.from_numpy(A, [a0, s, a]), a, DTensor.from_numpy(U, [a0, s, u]), u)
+    assert np.array_equal(Ax.to_numpy(), np.concatenate([A, U], axis=2))
+
+
+def test_errors_are_reported(nsg_ctx):
+    from networksolvers_gb300._native import NsgError
+    a, b = Index(3), Index(4)
+    T = DTensor.from_numpy(np.ones((3, 4)), [a, b])
+    with pytest.raises(NsgError):
+        it.factorize(T, [], cutoff=0.0)

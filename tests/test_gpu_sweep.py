@@ -1,0 +1,102 @@
+"""Whole-sweep parity on the GPU against the oracle and the golden fixtures.
+Tolerances (from the workload definition): energies 1e-10 relative, overlaps and
+fidelities 1e-8, truncated bond dimensions exactly equal."""
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+import networksolvers_gb300 as ns
+import networksolvers_gb300.models as m
+from networksolvers_gb300 import network as pn
+
+pytestmark = pytest.mark.gpu
+GOLD = Path(__file__).resolve().parent / "golden"
+
+
+def test_c1_heisenberg_n20_matches_golden(nsg_ctx):
+    gold = np.load(GOLD / "c1_heisenberg_n20.npz")
+    H, psi0 = m.config_heisenberg_chain(20, 10, 0)
+    rec = []
+
+    def cb(prob, sweep, region, which, **k):
+        rec.append((sweep, which, prob.eigenvalue, prob.last_insert.get("newdim", -1)))
+
+    E, psi = ns.dmrg(H, psi0, nsweeps=5, nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+                     inserter_kwargs=dict(trunc=dict(cutoff=1e-10, maxdim=64)), region_callback=cb)
+    rec = np.array(rec)
+    assert np.array_equal(rec[:, 3], gold["newdim"]), "truncated bond dimensions differ"
+    assert np.max(np.abs(rec[:, 2] - gold["eigenvalue"]) / np.abs(gold["eigenvalue"])) < 1e-10
+    assert abs(E - float(gold["energy"])) / abs(float(gold["energy"])) < 1e-10
+    assert abs(E - float(gold["ed_energy"])) < 1e-8
+    dims = psi.linkdims()
+    assert [dims[e] for e in H.graph.edges] == list(gold["linkdims"])
+
+
+def test_reference_tree_dmrg(nsg_ctx):
+    """test_tree_dmrg.jl:13-68 on the GPU: |E - E_ED| < 1e-5 for 2-site and for
+    1-site + densitymatrix expansion; parity with the oracle at 1e-10."""
+    gold = np.load(GOLD / "tree_dmrg.npz")
+    g = m.build_tree_graph(3, 3)
+    H, p0 = m.heisenberg_tree(g), m.neel_state(g)
+    trunc = dict(cutoff=1e-5, maxdim=40)
+    E2, _ = ns.dmrg(H, p0, nsweeps=5, nsites=2, inserter_kwargs=dict(trunc=trunc))
+    assert abs(E2 - float(gold["ed_energy"])) < 1e-5
+    assert abs(E2 - float(gold["e2"])) < 1e-10 * abs(E2)
+    E1, _ = ns.dmrg(H, p0, nsweeps=5, nsites=1, extracter_kwargs=dict(trunc=trunc, subspace_algorithm="densitymatrix"),
+                    inserter_kwargs=dict(trunc=trunc))
+    assert abs(E1 - float(gold["ed_energy"])) < 1e-5
+    assert abs(E1 - float(gold["e1"])) < 1e-10 * abs(E1)
+
+
+def _oracle_tdvp(H, psi0, times, nsites, solver):
+    from oracle import sweep as osw
+    uk = {} if solver == "rk4" else dict(solver=osw.exponentiate_solver)
+    return osw.tdvp(H, psi0, times, nsites=nsites, updater_kwargs=uk,
+                    inserter_kwargs=dict(trunc=dict(cutoff=1e-9, maxdim=64)))
+
+
+def _to_oracle(psi_dev, net_like):
+    from oracle import network as on
+    from networksolvers_gb300.models import Network
+    arrs = psi_dev.to_numpy(net_like)
+    return Network(net_like.graph, arrs, net_like.legs, np.complex128, {"kind": "state"})
+
+
+@pytest.mark.parametrize("nsites,solver", [(2, "expo"), (1, "rk4"), (2, "rk4")])
+def test_tfim_tree_tdvp_matches_oracle(nsg_ctx, nsites, solver):
+    """2-site/1-site TDVP, TFIM on a depth-2 binary tree from the all-up state:
+    fidelity with the oracle's state >= 1 - 1e-8."""
+    from oracle import network as on
+    g = m.binary_tree_graph(2)
+    H, psi0 = m.tfim_tree(g, h=1.0).astype(np.complex128), m.all_up_state(g)
+    times = [0.0, 0.05, 0.10, 0.15]
+    uk = {} if solver == "rk4" else dict(solver=ns.exponentiate_solver)
+    psi = ns.tdvp(H, psi0, times, nsites=nsites, updater_kwargs=uk,
+                  inserter_kwargs=dict(trunc=dict(cutoff=1e-9, maxdim=64)))
+    ref = _oracle_tdvp(H, psi0, times, nsites, solver)
+    got, _ = on.from_network(_to_oracle(psi, psi0), site_index={v: [i for i in ref[v].inds if i.tags.startswith("Site")][0]
+                                                                 for v in ref.g.vertices})
+    f = abs(on.inner(ref, got)) / (ref.norm() * got.norm())
+    assert f > 1 - 1e-8
+
+
+def test_tdvp_exact_evolution(nsg_ctx):
+    """2-site TDVP with exponentiate on a 7-site TFIM tree vs exact exp(-iHt)|ψ0>."""
+    from oracle import ed
+    g = m.binary_tree_graph(2)
+    H, psi0 = m.tfim_tree(g, h=1.0).astype(np.complex128), m.all_up_state(g)
+    times = np.arange(0, 0.2 + 1e-9, 0.05)
+    psi = ns.tdvp(H, psi0, times, nsites=2, updater_kwargs=dict(solver=ns.exponentiate_solver),
+                  inserter_kwargs=dict(trunc=dict(cutoff=1e-12, maxdim=64)))
+    terms = [(u, v, -1.0, m.PZ, m.PZ) for (u, v) in g.edges]
+    Hx = ed.hamiltonian(g.vertices, terms, {v: -1.0 * m.PX for v in g.vertices})
+    v0 = np.zeros(2 ** len(g.vertices), complex)
+    v0[0] = 1.0
+    vt = ed.evolve(Hx, v0, times[-1])
+    # contract the device state to a dense vector
+    from networksolvers_gb300.itensors import contract
+    full = contract([psi[v] for v in psi.g.vertices])
+    dense = full.permute([psi.siteind(v) for v in g.vertices]).to_numpy().reshape(-1)
+    fid = abs(np.vdot(vt, dense)) / np.linalg.norm(dense)
+    assert fid > 1 - 1e-8
