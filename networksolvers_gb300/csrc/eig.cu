@@ -35,8 +35,9 @@ __device__ __forceinline__ double abs_(double2 v) { return hypot(v.x, v.y); }
 
 // rotate a pair (x_p, x_q) with J = [[c, s], [-s e, c e]] where e = conj(phase) (columns)
 // For real data phase = 1.
-__device__ __forceinline__ void rot_cols(double& xp, double& xq, double c, double s, double2) {
-  double a = xp, b = xq;
+__device__ __forceinline__ void rot_cols(double& xp, double& xq, double c, double s, double2 e) {
+  // real case: e = sign(G_pq)
+  double a = xp, b = e.x * xq;
   xp = c * a - s * b;
   xq = s * a + c * b;
 }
@@ -47,8 +48,8 @@ __device__ __forceinline__ void rot_cols(double2& xp, double2& xq, double c, dou
   xp = make_double2(c * a.x - s * eb.x, c * a.y - s * eb.y);
   xq = make_double2(s * a.x + c * eb.x, s * a.y + c * eb.y);
 }
-__device__ __forceinline__ void rot_rows(double& xp, double& xq, double c, double s, double2) {
-  double a = xp, b = xq;
+__device__ __forceinline__ void rot_rows(double& xp, double& xq, double c, double s, double2 e) {
+  double a = xp, b = e.x * xq;
   xp = c * a - s * b;
   xq = s * a + c * b;
 }
@@ -60,7 +61,7 @@ __device__ __forceinline__ void rot_rows(double2& xp, double2& xq, double c, dou
   xp = make_double2(c * a.x - s * eb.x, c * a.y - s * eb.y);
   xq = make_double2(s * a.x + c * eb.x, s * a.y + c * eb.y);
 }
-__device__ __forceinline__ double2 phase_of(double b) { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ double2 phase_of(double b) { return make_double2(b >= 0 ? 1.0 : -1.0, 0.0); }
 __device__ __forceinline__ double2 phase_of(double2 b) {
   double r = hypot(b.x, b.y);
   return r > 0 ? make_double2(b.x / r, -b.y / r) : make_double2(1.0, 0.0);  // exp(-i phi)

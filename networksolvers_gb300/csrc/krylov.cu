@@ -82,6 +82,44 @@ void tridiag_eig(int n, const double* alpha, const double* beta, double* evals, 
   for (size_t i = 0; i < size_t(n) * n; ++i) evecs[i] = V[i];
 }
 
+// exp(A) of a small complex k x k matrix (column-major): scaling and squaring with a
+// degree-18 Taylor polynomial on A / 2^s, ||A / 2^s||_1 <= 1/2.  Tiny entries (the
+// Krylov error corner) keep their relative accuracy.
+static std::vector<std::complex<double>> expm_small(int k, const std::vector<std::complex<double>>& A) {
+  using cd = std::complex<double>;
+  double nrm = 0.0;
+  for (int j = 0; j < k; ++j) {
+    double c = 0.0;
+    for (int i = 0; i < k; ++i) c += std::abs(A[i + size_t(k) * j]);
+    nrm = std::max(nrm, c);
+  }
+  int s = nrm <= 0.5 ? 0 : int(std::ceil(std::log2(nrm / 0.5)));
+  double sc = std::ldexp(1.0, -s);
+  std::vector<cd> X(A.size()), E(A.size(), cd(0, 0)), term(A.size(), cd(0, 0)), tmp(A.size());
+  for (size_t i = 0; i < A.size(); ++i) X[i] = A[i] * sc;
+  for (int i = 0; i < k; ++i) E[i + size_t(k) * i] = term[i + size_t(k) * i] = cd(1, 0);
+  auto matmul = [&](const std::vector<cd>& P, const std::vector<cd>& Q, std::vector<cd>& R) {
+    for (int j = 0; j < k; ++j)
+      for (int i = 0; i < k; ++i) {
+        cd acc(0, 0);
+        for (int l = 0; l < k; ++l) acc += P[i + size_t(k) * l] * Q[l + size_t(k) * j];
+        R[i + size_t(k) * j] = acc;
+      }
+  };
+  for (int j = 1; j <= 18; ++j) {
+    matmul(term, X, tmp);
+    for (size_t i = 0; i < tmp.size(); ++i) {
+      term[i] = tmp[i] / double(j);
+      E[i] += term[i];
+    }
+  }
+  for (int q = 0; q < s; ++q) {
+    matmul(E, E, tmp);
+    E.swap(tmp);
+  }
+  return E;
+}
+
 namespace {
 
 struct Vecs {
@@ -208,11 +246,13 @@ int nsg_exponentiate(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_te
     double err = INFINITY;
     int k = 0;
     auto expm_col = [&](int kk, cd tau, std::vector<cd>& col) {
-      std::vector<double> ev(kk), Q(size_t(kk) * kk);
-      tridiag_eig(kk, alpha.data(), beta.data(), ev.data(), Q.data());
-      col.assign(kk, cd(0, 0));
-      for (int i = 0; i < kk; ++i)
-        for (int l = 0; l < kk; ++l) col[i] += Q[i + size_t(kk) * l] * std::exp(tau * ev[l]) * Q[0 + size_t(kk) * l];
+      std::vector<cd> A(size_t(kk) * kk, cd(0, 0));
+      for (int i = 0; i < kk; ++i) {
+        A[i + size_t(kk) * i] = tau * alpha[i];
+        if (i + 1 < kk) A[i + size_t(kk) * (i + 1)] = A[(i + 1) + size_t(kk) * i] = tau * beta[i];
+      }
+      std::vector<cd> E2 = expm_small(kk, A);
+      col.assign(E2.begin(), E2.begin() + kk);
     };
     for (int j = 0; j < krylovdim; ++j) {
       double a, b;
@@ -229,14 +269,23 @@ int nsg_exponentiate(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_te
     }
     cd step = remaining;
     if (!(err <= tol || beta[k - 1] <= tol * 1e-3)) {
-      double s = 0.5;
-      while (true) {
-        step = remaining * s;
-        expm_col(k, step, E);
-        double e2 = beta0 * beta[k - 1] * std::abs(E[k - 1]);
-        if (e2 <= tol * std::abs(step) / std::abs(t) || s < 1e-12) break;
-        s *= 0.5;
+      // largest fraction of the remaining step within the per-unit-time error budget
+      auto est = [&](double s, std::vector<cd>& col) {
+        expm_col(k, remaining * s, col);
+        return beta0 * beta[k - 1] * std::abs(col[k - 1]);
+      };
+      double lo = 0.0, hi = 1.0;
+      std::vector<cd> tmp;
+      for (int b = 0; b < 50; ++b) {
+        double mid = 0.5 * (lo + hi);
+        if (est(mid, tmp) <= tol * mid * std::abs(remaining) / std::abs(t))
+          lo = mid;
+        else
+          hi = mid;
       }
+      if (lo <= 0.0) break;
+      step = remaining * lo;
+      est(lo, E);
     }
     std::vector<double> coef(2 * k);
     for (int j = 0; j < k; ++j) {

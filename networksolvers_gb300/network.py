@@ -340,7 +340,12 @@ class ProjTTN:
         inc = [self.environment(psi, w, u) for w in self.g.neighbors(u) if w != v]
         A = psi[u]
         bra = A.dag().prime()
-        lk = psi.linkind(u, v)
+        # the bond index of A toward v: not its site index, not a link to another neighbour
+        # (psi[v] may temporarily carry a different bond index, as in the 1-site TDVP
+        # back-evolution where psi[u] = Q from a fresh QR)
+        others = {psi.linkind(u, w) for w in self.g.neighbors(u) if w != v}
+        site = psi.siteind(u)
+        lk = [i for i in A.inds if i != site and i not in others][0]
         # output order [link', oplink, link] — the layout the chain kernels read
         hl = commonind(self.H[u], self.H[v])
         T = contract([A] + inc + [self.H[u], bra], out=[lk.prime(), hl, lk])

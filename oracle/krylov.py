@@ -11,8 +11,9 @@
 * `exponentiate` — Lanczos exponential integrator for exp(t·A)·x with A Hermitian
   (local_solvers/exponentiate.jl:16-27): grow the basis one vector at a time
   (eager), accept the full remaining step when the estimate
-  ‖x‖·|β_k|·|[exp(τT_k)]_{k,1}| ≤ tol; at krylovdim take the largest step τ·2^-j
-  whose estimate is ≤ tol·|τ_step|/|t| and restart from the advanced vector.
+  ‖x‖·|β_k|·|[exp(τT_k)]_{k,1}| ≤ tol; at krylovdim take the largest fraction of the
+  remaining step (bisection, 50 halvings) whose estimate is ≤ tol·|τ_step|/|t| and
+  restart from the advanced vector.
 * `runge_kutta_2/4`, `runge_kutta_solver` — runge_kutta.jl:2-25, verbatim algebra.
 """
 from __future__ import annotations
@@ -80,9 +81,27 @@ def eigsolve_lanczos(A, x0, krylovdim=3, maxiter=1, tol=1e-14):
     return lam, x
 
 
+def expm_small(A):
+    """exp(A) of a small complex matrix: scaling and squaring with a degree-18 Taylor
+    polynomial on A/2^s, ||A/2^s||_1 <= 1/2.  Entries that are tiny (the Krylov error
+    corner [k-1, 0]) keep their relative accuracy, which an eigendecomposition does not."""
+    A = np.asarray(A, dtype=np.complex128)
+    k = A.shape[0]
+    nrm = np.abs(A).sum(axis=0).max() if k else 0.0
+    s = 0 if nrm <= 0.5 else int(np.ceil(np.log2(nrm / 0.5)))
+    X = A / (2.0 ** s)
+    E = np.eye(k, dtype=np.complex128)
+    term = np.eye(k, dtype=np.complex128)
+    for j in range(1, 19):
+        term = (term @ X) / j
+        E = E + term
+    for _ in range(s):
+        E = E @ E
+    return E
+
+
 def _expm_sym_tridiag(T, tau):
-    w, Q = np.linalg.eigh(T)
-    return (Q * np.exp(tau * w)) @ Q.T
+    return expm_small(tau * T)
 
 
 def exponentiate(A, t, x, krylovdim=30, maxiter=100, tol=1e-12):
@@ -116,15 +135,25 @@ def exponentiate(A, t, x, krylovdim=30, maxiter=100, tol=1e-12):
             step = remaining
             E = state["E"]
         else:
+            # largest fraction s of the remaining time whose estimate is within the
+            # per-unit-time budget tol*|step|/|t| (bisection, 50 halvings)
             T = _tridiag(alpha, beta[:-1])
-            s = 0.5
-            while True:
-                step = remaining * s
-                E = _expm_sym_tridiag(T, step)
-                err = beta0 * abs(beta[-1]) * abs(E[k - 1, 0])
-                if err <= tol * abs(step) / abs(t) or s < 1e-12:
-                    break
-                s *= 0.5
+
+            def est(s):
+                Es = expm_small(remaining * s * T)[:, 0]
+                return Es, beta0 * abs(beta[-1]) * abs(Es[k - 1])
+
+            lo, hi = 0.0, 1.0
+            for _ in range(50):
+                mid = 0.5 * (lo + hi)
+                if est(mid)[1] <= tol * mid * abs(remaining) / abs(t):
+                    lo = mid
+                else:
+                    hi = mid
+            if lo <= 0.0:
+                return w, {"converged": False, "numops": numops}
+            step = remaining * lo
+            E = est(lo)[0][:, None]
         coef = beta0 * E[:, 0]
         w = sum(c * v for c, v in zip(coef, V))
         remaining = remaining - step
