@@ -78,6 +78,10 @@ template <typename T>
 __global__ void __launch_bounds__(kJacobiThreads)
     jacobi_kernel(T* __restrict__ G, int n, T* __restrict__ V, double* __restrict__ w, int max_sweeps,
                   int* __restrict__ sweeps_out) {
+  // batched: CTA b works on matrix b (consecutive n x n blocks)
+  G += (size_t)blockIdx.x * n * n;
+  V += (size_t)blockIdx.x * n * n;
+  w += (size_t)blockIdx.x * n;
   __shared__ double cs_[kJacobiMaxN / 2], sn_[kJacobiMaxN / 2];
   __shared__ double2 ph_[kJacobiMaxN / 2];
   __shared__ int p_[kJacobiMaxN / 2], q_[kJacobiMaxN / 2];
@@ -177,7 +181,7 @@ __global__ void __launch_bounds__(kJacobiThreads)
     __syncthreads();
   }
   for (int i = tid; i < n; i += nt) w[i] = re_(G[i + int64_t(n) * i]);
-  if (tid == 0 && sweeps_out) *sweeps_out = sweep;
+  if (tid == 0 && sweeps_out) sweeps_out[blockIdx.x] = sweep;
 }
 
 struct Spectrum {
@@ -264,6 +268,14 @@ nsg_tensor* matricize(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int
 
 }  // namespace
 
+void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* w) {
+  NSG_CHECK(n >= 1 && n <= kJacobiMaxN && batch >= 1, NSG_ERR_INVALID, "jacobi_batched: bad size");
+  int threads = n <= 64 ? 128 : kJacobiThreads;
+  jacobi_kernel<double><<<batch, threads, 0, c->stream>>>(A, n, V, w, 60, nullptr);
+  count_launch(c);
+  check_launch("jacobi_batched");
+}
+
 void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev) {
   NSG_CHECK(n >= 1 && n <= kJacobiMaxN, NSG_ERR_UNSUPPORTED,
             "eigensolver: matrix order " + std::to_string(n) + " above the supported maximum");
@@ -274,19 +286,6 @@ void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev) {
     jacobi_kernel<double><<<1, threads, 0, c->stream>>>((double*)A, int(n), (double*)V, w_dev, 60, nullptr);
   count_launch(c);
   check_launch("jacobi");
-}
-
-// Hermitian eigendecomposition of an m x m matrix stored in `Mat` (column-major,
-// consumed): returns sorted spectrum and the eigenvector matrix Z (device).
-static void gram_eig(nsg_ctx* c, int dtype, int64_t m, void* Mat, void* Z, Spectrum& sp) {
-  double* wdev = (double*)dalloc(c, sizeof(double) * m);
-  syevd(c, dtype, m, Mat, Z, wdev);
-  std::vector<double> w(m);
-  NSG_CUDA(cudaMemcpyAsync(w.data(), wdev, sizeof(double) * m, cudaMemcpyDeviceToHost, c->stream));
-  NSG_CUDA(cudaStreamSynchronize(c->stream));
-  dfree(c, wdev, sizeof(double) * m);
-  for (double x : w) NSG_CHECK(std::isfinite(x), NSG_ERR_NONFINITE, "eigensolver: non-finite eigenvalue");
-  sp = sorted_spectrum(w);
 }
 
 }  // namespace nsg
@@ -305,7 +304,8 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   nsg_tensor* M = matricize(c, T, left_axes, n_left, &m, &ncol, ldims, rdims, &owned);
   const int dt = T->dtype;
   const size_t eb = elem_bytes(dt);
-  // G = M M^H
+  NSG_CHECK(m <= (1 << 16), NSG_ERR_UNSUPPORTED, "factorize: row space above 65536");
+  // G = M M^H (FP64 in every precision mode: the Gram matrix fixes the truncation)
   void* G = dalloc(c, eb * m * m);
   GemmArgs g;
   g.dtype = dt;
@@ -322,23 +322,35 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   g.ldc = m;
   g.batch = 1;
   g.strideA = g.strideB = g.strideC = 0;
-  gemm_f64_simt(c, g);  // the Gram matrix and its eigenvectors stay FP64 in every precision mode
-  void* Z = dalloc(c, eb * m * m);
-  Spectrum sp;
-  gram_eig(c, dt, m, G, Z, sp);
-  dfree(c, G, eb * m * m);
-  int64_t origm = std::min(m, ncol);
+  gemm_f64_simt(c, g);
+  const int64_t origm = std::min(m, ncol);
   double err = 0.0;
-  int64_t k = truncate_rule(sp.P, origm, cutoff, maxdim, mindim, &err);
-  // U = Z[:, order[0..k)]
-  std::vector<int64_t> udims = ldims;
-  udims.push_back(k);
-  nsg_tensor* Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
-  int* didx = (int*)dalloc(c, sizeof(int) * k);
-  NSG_CUDA(cudaMemcpyAsync(didx, sp.order.data(), sizeof(int) * k, cudaMemcpyHostToDevice, c->stream));
-  copy_columns(c, dt, m, k, Z, m, didx, Ut->data, m);
-  dfree(c, didx, sizeof(int) * k);
-  dfree(c, Z, eb * m * m);
+  int64_t k = 0;
+  nsg_tensor* Ut = nullptr;
+  std::vector<double> P;
+  std::vector<double> w;
+  PickFn pick = [&](const std::vector<double>& wa, void** Z, int64_t* ldz) {
+    // descending spectrum
+    P.assign(wa.rbegin(), wa.rend());
+    k = truncate_rule(P, origm, cutoff, maxdim, mindim, &err);
+    std::vector<int64_t> udims = ldims;
+    udims.push_back(k);
+    Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+    *Z = Ut->data;
+    *ldz = m;
+    std::vector<int> cols(k);
+    for (int64_t i = 0; i < k; ++i) cols[i] = int(m - 1 - i);
+    return cols;
+  };
+  try {
+    syevd_dc(c, dt, int(m), G, w, pick);
+  } catch (...) {
+    dfree(c, G, eb * m * m);
+    if (Ut) free_tensor(c, Ut);
+    if (owned) free_tensor(c, M);
+    throw;
+  }
+  dfree(c, G, eb * m * m);
   // C = U^H M
   std::vector<int64_t> cdims;
   cdims.push_back(k);
@@ -363,7 +375,7 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   if (owned) free_tensor(c, M);
   if (spectrum)
     for (int64_t i = 0; i < std::min<int64_t>(spectrum_cap, origm); ++i)
-      spectrum[i] = i < int64_t(sp.P.size()) ? std::max(sp.P[i], 0.0) : 0.0;
+      spectrum[i] = i < int64_t(P.size()) ? std::max(P[i], 0.0) : 0.0;
   *U = Ut;
   *C = Ct;
   if (newdim) *newdim = k;
@@ -400,23 +412,32 @@ int nsg_eigh(nsg_ctx* c, const nsg_tensor* rho, const int* row_axes, int n_row, 
   void* A = dalloc(c, eb * m * m);
   NSG_CUDA(cudaMemcpyAsync(A, M->data, eb * m * m, cudaMemcpyDeviceToDevice, c->stream));
   if (owned) free_tensor(c, M);
-  void* Z = dalloc(c, eb * m * m);
-  Spectrum sp;
-  gram_eig(c, dt, m, A, Z, sp);
-  dfree(c, A, eb * m * m);
   double err = 0.0;
-  int64_t k = truncate_rule(sp.P, m, cutoff, maxdim, mindim, &err);
-  std::vector<int64_t> udims = rdims;
-  udims.push_back(k);
-  nsg_tensor* Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
-  int* didx = (int*)dalloc(c, sizeof(int) * k);
-  NSG_CUDA(cudaMemcpyAsync(didx, sp.order.data(), sizeof(int) * k, cudaMemcpyHostToDevice, c->stream));
-  copy_columns(c, dt, m, k, Z, m, didx, Ut->data, m);
-  NSG_CUDA(cudaStreamSynchronize(c->stream));
-  dfree(c, didx, sizeof(int) * k);
-  dfree(c, Z, eb * m * m);
+  int64_t k = 0;
+  nsg_tensor* Ut = nullptr;
+  std::vector<double> P, w;
+  PickFn pick = [&](const std::vector<double>& wa, void** Z, int64_t* ldz) {
+    P.assign(wa.rbegin(), wa.rend());
+    k = truncate_rule(P, m, cutoff, maxdim, mindim, &err);
+    std::vector<int64_t> udims = rdims;
+    udims.push_back(k);
+    Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+    *Z = Ut->data;
+    *ldz = m;
+    std::vector<int> cols(k);
+    for (int64_t i = 0; i < k; ++i) cols[i] = int(m - 1 - i);
+    return cols;
+  };
+  try {
+    syevd_dc(c, dt, int(m), A, w, pick);
+  } catch (...) {
+    dfree(c, A, eb * m * m);
+    if (Ut) free_tensor(c, Ut);
+    throw;
+  }
+  dfree(c, A, eb * m * m);
   if (evals)
-    for (int64_t i = 0; i < std::min(evals_cap, k); ++i) evals[i] = sp.P[i];
+    for (int64_t i = 0; i < std::min(evals_cap, k); ++i) evals[i] = P[i];
   *U = Ut;
   if (newdim) *newdim = k;
   if (truncerr) *truncerr = err;

@@ -6,6 +6,7 @@
 #include <cstdio>
 #include <string>
 #include <vector>
+#include <functional>
 #include <stdexcept>
 
 #include "../../include/nsg.h"
@@ -116,6 +117,12 @@ void row_norms2(nsg_ctx* c, int dtype, int64_t rows, int64_t cols, const void* A
 // symmetric/Hermitian eigen of a dense n x n matrix (column-major, overwritten);
 // eigenvectors to V (n x n), eigenvalues (unsorted) to w_dev.
 void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev);
+
+// Hermitian eigensolver (tridiagonalisation + divide and conquer + back-transformation).
+// A (n x n) is consumed.  `pick` receives the eigenvalues in ascending order and returns
+// the indices whose eigenvectors are wanted, after pointing *Z / *ldz at the output.
+using PickFn = std::function<std::vector<int>(const std::vector<double>&, void** Z, int64_t* ldz)>;
+void syevd_dc(nsg_ctx* c, int dtype, int n, void* A, std::vector<double>& w_host, const PickFn& pick);
 
 // host helpers
 void tridiag_eig(int n, const double* alpha, const double* beta, double* evals, double* evecs);

@@ -1,0 +1,1014 @@
+// Dense Hermitian eigensolver for the truncated factorizations:
+//   1. Householder reduction to a real symmetric tridiagonal T (one cooperative
+//      kernel, two grid barriers per column; the matrix stays L2-resident),
+//   2. Cuppen divide and conquer on T: Jacobi leaves of <= 32, rank-one merges with
+//      deflation (small z / close poles), secular roots by bracketed Newton with the
+//      origin at the nearer pole (one thread per root over many CTAs), Gu-Eisenstat
+//      recomputed z for orthogonal vectors, merged by an FP64 GEMM,
+//   3. back-transformation of the kept eigenvectors with the Householder reflectors
+//      in blocks of 32 (compact WY, three GEMMs per block).
+// Every wait in these kernels is bounded: the grid barrier gives up after ~2^26
+// polls, raises an error flag and the host reports NSG_ERR_TIMEOUT.
+#include "nsg_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <functional>
+#include <numeric>
+
+namespace nsg {
+
+void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* w);  // eig.cu
+
+namespace {
+
+constexpr int kTriThreads = 256;
+constexpr int kLeaf = 32;
+
+__device__ __forceinline__ double cre(double v) { return v; }
+__device__ __forceinline__ double cre(double2 v) { return v.x; }
+__device__ __forceinline__ double cabs2(double v) { return v * v; }
+__device__ __forceinline__ double cabs2(double2 v) { return v.x * v.x + v.y * v.y; }
+__device__ __forceinline__ double cconj(double v) { return v; }
+__device__ __forceinline__ double2 cconj(double2 v) { return make_double2(v.x, -v.y); }
+__device__ __forceinline__ double cmulv(double a, double b) { return a * b; }
+__device__ __forceinline__ double2 cmulv(double2 a, double2 b) {
+  return make_double2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ double cscale(double a, double s) { return a * s; }
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+__device__ __forceinline__ double cadd(double a, double b) { return a + b; }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double csub(double a, double b) { return a - b; }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+template <typename T>
+__device__ __forceinline__ T czero();
+template <>
+__device__ __forceinline__ double czero<double>() { return 0.0; }
+template <>
+__device__ __forceinline__ double2 czero<double2>() { return make_double2(0.0, 0.0); }
+template <typename T>
+__device__ __forceinline__ T cone();
+template <>
+__device__ __forceinline__ double cone<double>() { return 1.0; }
+template <>
+__device__ __forceinline__ double2 cone<double2>() { return make_double2(1.0, 0.0); }
+__device__ __forceinline__ double cdiv(double a, double b) { return a / b; }
+__device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
+  double den = b.x * b.x + b.y * b.y;
+  return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+// Grid barrier with a bounded wait (cooperative launch guarantees co-residency).
+struct Barrier {
+  unsigned int count;
+  unsigned int gen;
+  int err;
+};
+
+__device__ bool grid_sync(Barrier* b) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned int* vgen = &b->gen;
+    unsigned int g = *vgen;
+    __threadfence();
+    unsigned int arrived = atomicAdd(&b->count, 1u);
+    if (arrived == gridDim.x - 1) {
+      b->count = 0;
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      long long polls = 0;
+      while (*vgen == g) {
+        if (++polls > (1ll << 26) || *(volatile int*)&b->err) {
+          atomicExch(&b->err, 1);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    s_ok = (*(volatile int*)&b->err) == 0;
+  }
+  __syncthreads();
+  return s_ok;
+}
+
+template <typename T>
+__device__ T block_sum(T v, T* red) {
+  // sum over the block; result valid in every thread
+  for (int o = 16; o > 0; o >>= 1) {
+    if constexpr (sizeof(T) == 8) {
+      v += __shfl_down_sync(0xffffffffu, v, o);
+    } else {
+      double2 t;
+      t.x = __shfl_down_sync(0xffffffffu, ((double2&)v).x, o);
+      t.y = __shfl_down_sync(0xffffffffu, ((double2&)v).y, o);
+      v = cadd(v, *(T*)&t);
+    }
+  }
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  T s = czero<T>();
+  for (int k = 0; k < int(blockDim.x + 31) / 32; ++k) s = cadd(s, red[k]);
+  __syncthreads();
+  return s;
+}
+
+// Householder tridiagonalisation of the Hermitian n x n matrix A (column-major, both
+// triangles stored).  On exit d[k] = T_kk, e[k] = T_k,k+1 (real), tau[k], and the
+// reflector vectors v_k (v_k[k+1] = 1 implicit) below the subdiagonal of column k.
+// Update per column: x = tau A22 v, w = x - tau/2 (x^H v) v, A22 -= v w^H + w v^H.
+template <typename T>
+__global__ void __launch_bounds__(kTriThreads)
+    tridiag_kernel(T* __restrict__ A, int n, double* __restrict__ d, double* __restrict__ e, T* __restrict__ tau,
+                   T* __restrict__ xbuf, T* __restrict__ partial, Barrier* bar) {
+  extern __shared__ unsigned char smem_raw[];
+  T* v = (T*)smem_raw;  // n entries
+  __shared__ T red[kTriThreads / 32];
+  const int tid = threadIdx.x, nt = blockDim.x, nb = gridDim.x, b = blockIdx.x;
+  const int gtid = b * nt + tid, gnt = nb * nt;
+  const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
+  const int gwarp = b * nwarps + warp, gnwarps = nb * nwarps;
+  for (int k = 0; k < n - 2; ++k) {
+    const int m = n - k - 1;  // active size (rows k+1..n-1)
+    T* col = A + (size_t)k * n;
+    // every CTA reads column k and forms the reflector redundantly (same order -> same bits)
+    double ss = 0.0;
+    for (int i = k + 2 + tid; i < n; i += nt) ss += cabs2(col[i]);
+    double xnorm2 = block_sum<double>(ss, (double*)red);
+    T alpha = col[k + 1];
+    double ar = cre(alpha);
+    double ai = 0.0;
+    if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
+    T tk = czero<T>();
+    double beta = ar;
+    T scale = czero<T>();
+    bool active = !(xnorm2 == 0.0 && ai == 0.0);
+    if (active) {
+      double nrm = sqrt(ar * ar + ai * ai + xnorm2);
+      beta = ar >= 0 ? -nrm : nrm;
+      if constexpr (sizeof(T) == 16) {
+        double2 t2 = make_double2((beta - ar) / beta, -ai / beta);
+        tk = *(T*)&t2;
+        double2 am = make_double2(ar - beta, ai);
+        double2 inv = cdiv(make_double2(1.0, 0.0), am);
+        scale = *(T*)&inv;
+      } else {
+        double t1 = (beta - ar) / beta;
+        tk = *(T*)&t1;
+        double s1 = 1.0 / (ar - beta);
+        scale = *(T*)&s1;
+      }
+    }
+    // v in shared memory (indices 0..m-1 <-> rows k+1..n-1)
+    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? cone<T>() : cmulv(col[k + 1 + i], scale);
+    __syncthreads();
+    if (b == 0 && tid == 0) {
+      d[k] = cre(A[k + (size_t)k * n]);
+      e[k] = active ? beta : ar;
+      tau[k] = tk;
+    }
+    if (!active) {
+      // H = I; keep column k as is (e[k] = Re(alpha), alpha real) and move on
+      if (!grid_sync(bar)) return;
+      continue;
+    }
+    // x = tau * A22 * v   (row i of A22 = conj(column i) by symmetry: coalesced column reads)
+    double2 pacc = make_double2(0.0, 0.0);
+    for (int i = gwarp; i < m; i += gnwarps) {
+      const T* ci = A + (size_t)(k + 1 + i) * n + (k + 1);
+      T acc = czero<T>();
+      for (int j = lane; j < m; j += 32) acc = cadd(acc, cmulv(cconj(ci[j]), v[j]));
+      for (int o = 16; o > 0; o >>= 1) {
+        if constexpr (sizeof(T) == 8) {
+          acc += __shfl_down_sync(0xffffffffu, acc, o);
+        } else {
+          double2 t;
+          t.x = __shfl_down_sync(0xffffffffu, ((double2&)acc).x, o);
+          t.y = __shfl_down_sync(0xffffffffu, ((double2&)acc).y, o);
+          acc = cadd(acc, *(T*)&t);
+        }
+      }
+      if (lane == 0) {
+        T xi = cmulv(tk, acc);
+        xbuf[i] = xi;
+        // accumulate x^H v
+        T p = cmulv(cconj(xi), v[i]);
+        if constexpr (sizeof(T) == 8) {
+          pacc.x += (double&)p;
+        } else {
+          pacc.x += ((double2&)p).x;
+          pacc.y += ((double2&)p).y;
+        }
+      }
+    }
+    // per-CTA partial of x^H v in fixed order: per-warp slot, then CTA sum
+    __shared__ double2 wsum[kTriThreads / 32];
+    if (lane == 0) wsum[warp] = pacc;
+    __syncthreads();
+    if (tid == 0) {
+      double2 s = make_double2(0.0, 0.0);
+      for (int w = 0; w < nwarps; ++w) {
+        s.x += wsum[w].x;
+        s.y += wsum[w].y;
+      }
+      ((double2*)partial)[b] = s;
+    }
+    if (!grid_sync(bar)) return;
+    // x^H v: every CTA sums the partials in the same order
+    double2 xv = make_double2(0.0, 0.0);
+    for (int q = 0; q < nb; ++q) {
+      xv.x += ((double2*)partial)[q].x;
+      xv.y += ((double2*)partial)[q].y;
+    }
+    // alpha2 = -tau/2 * (x^H v); w = x + alpha2 v
+    T xvT;
+    if constexpr (sizeof(T) == 8) {
+      double t1 = xv.x;
+      xvT = *(T*)&t1;
+    } else {
+      xvT = *(T*)&xv;
+    }
+    T alpha2 = cscale(cmulv(tk, xvT), -0.5);
+    // rank-2 update of A22 (both triangles): A[i, j] -= v_i conj(w_j) + w_i conj(v_j)
+    const size_t mm = (size_t)m * m;
+    for (size_t t = gtid; t < mm; t += gnt) {
+      int i = int(t % m), j = int(t / m);
+      T wi = cadd(xbuf[i], cmulv(alpha2, v[i]));
+      T wj = cadd(xbuf[j], cmulv(alpha2, v[j]));
+      T* p = A + (size_t)(k + 1 + j) * n + (k + 1 + i);
+      *p = csub(*p, cadd(cmulv(v[i], cconj(wj)), cmulv(wi, cconj(v[j]))));
+    }
+    // store the reflector below the subdiagonal (column k is no longer read)
+    if (b == nb - 1)
+      for (int i = tid + 1; i < m; i += nt) col[k + 1 + i] = v[i];
+    if (!grid_sync(bar)) return;
+  }
+  if (b == 0 && tid == 0) {
+    if (n >= 2) {
+      d[n - 2] = cre(A[(n - 2) + (size_t)(n - 2) * n]);
+      e[n - 2] = cre(A[(n - 1) + (size_t)(n - 2) * n]);
+    }
+    d[n - 1] = cre(A[(n - 1) + (size_t)(n - 1) * n]);
+  }
+}
+
+// For complex A the last subdiagonal element may be complex: handled on the host by a
+// unitary diagonal scaling (phase folded into the back-transformation).
+
+// ---------------------------------------------------------------------------
+// divide and conquer
+// ---------------------------------------------------------------------------
+
+struct MergeDesc {
+  int lo, mid, hi;
+  double beta;
+};
+
+// Build dense leaf matrices (kLeaf x kLeaf, zero padded with distinct large diagonal
+// entries that are removed afterwards) from the modified tridiagonal.
+__global__ void leaf_build_kernel(const double* d, const double* e, const int* leaf_lo, const int* leaf_hi,
+                                  int nleaf, double* M) {
+  int L = blockIdx.x;
+  if (L >= nleaf) return;
+  int lo = leaf_lo[L], hi = leaf_hi[L], s = hi - lo;
+  double* A = M + (size_t)L * kLeaf * kLeaf;
+  for (int t = threadIdx.x; t < kLeaf * kLeaf; t += blockDim.x) {
+    int i = t % kLeaf, j = t / kLeaf;
+    double v = 0.0;
+    if (i < s && j < s) {
+      if (i == j)
+        v = d[lo + i];
+      else if (j == i + 1)
+        v = e[lo + i];
+      else if (i == j + 1)
+        v = e[lo + j];
+    }
+    A[t] = v;
+  }
+}
+
+// Scatter leaf eigenpairs into Q (n x n, column-major) and w, sorted ascending.
+__global__ void leaf_scatter_kernel(const double* M, const double* V, const double* wl, const int* leaf_lo,
+                                    const int* leaf_hi, int nleaf, double* Q, int n, double* w) {
+  int L = blockIdx.x;
+  if (L >= nleaf) return;
+  int lo = leaf_lo[L], hi = leaf_hi[L], s = hi - lo;
+  const double* Vl = V + (size_t)L * kLeaf * kLeaf;
+  const double* wv = wl + (size_t)L * kLeaf;
+  __shared__ int order[kLeaf];
+  if (threadIdx.x == 0) {
+    // eigenpairs that belong to the leaf: the padding rows/cols are zero, so the
+    // padded eigenvectors are unit vectors on indices >= s; pick vectors with support < s
+    int cnt = 0;
+    int idx[kLeaf];
+    for (int j = 0; j < kLeaf; ++j) {
+      double tail = 0.0;
+      for (int i = s; i < kLeaf; ++i) tail += fabs(Vl[i + j * kLeaf]);
+      if (tail < 0.5 && cnt < s) idx[cnt++] = j;
+    }
+    // insertion sort by eigenvalue
+    for (int a = 1; a < cnt; ++a) {
+      int x = idx[a];
+      int b = a - 1;
+      while (b >= 0 && wv[idx[b]] > wv[x]) {
+        idx[b + 1] = idx[b];
+        --b;
+      }
+      idx[b + 1] = x;
+    }
+    for (int a = 0; a < s; ++a) order[a] = a < cnt ? idx[a] : 0;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < s * s; t += blockDim.x) {
+    int i = t % s, j = t / s;
+    Q[(size_t)(lo + j) * n + (lo + i)] = Vl[i + order[j] * kLeaf];
+  }
+  for (int j = threadIdx.x; j < s; j += blockDim.x) w[lo + j] = wv[order[j]];
+}
+
+// Per merge (one CTA, serial parts on thread 0): gather D and z, flip for rho < 0,
+// sort, normalise z, deflate.  Outputs (per merge, arrays of length nb = hi - lo, at
+// offset lo in the workspace):
+//   Ds[a]   sorted (flipped) poles, perm[a] local column of sorted slot a
+//   zs[a]   normalised z (0 for deflated)
+//   kind[a] 1 = non-deflated, 0 = deflated
+//   rot     Givens list (local cols p, q, c, s) in application order
+// and scalars: rho (after normalisation), k, nrot, flip.
+struct MergeWork {
+  double* Ds;
+  double* zs;
+  int* perm;
+  int* kind;
+  int* rot_pq;     // 2 per rotation
+  double* rot_cs;  // 2 per rotation
+  double* rho;     // per merge
+  int* counts;     // per merge: k, nrot, flip
+};
+
+__global__ void merge_prep_kernel(const double* w, const double* Q, int n, const MergeDesc* md, int nmerge,
+                                  MergeWork W) {
+  int mi = blockIdx.x;
+  if (mi >= nmerge || threadIdx.x != 0) return;
+  const MergeDesc M = md[mi];
+  const int lo = M.lo, mid = M.mid, hi = M.hi, nb = hi - lo, n1 = mid - lo;
+  double rho = M.beta;
+  int flip = rho < 0;
+  double sg = flip ? -1.0 : 1.0;
+  if (flip) rho = -rho;
+  double* Ds = W.Ds + lo;
+  double* zs = W.zs + lo;
+  int* perm = W.perm + lo;
+  int* kind = W.kind + lo;
+  // merge the two ascending halves after the sign flip (descending halves when flipped)
+  int a = 0, b = 0;
+  for (int t = 0; t < nb; ++t) {
+    int ia = flip ? (n1 - 1 - a) : a;         // local index into half 1
+    int ib = flip ? (nb - 1 - b) : (n1 + b);  // local index into half 2
+    bool takeA;
+    if (a >= n1)
+      takeA = false;
+    else if (b >= nb - n1)
+      takeA = true;
+    else
+      takeA = sg * w[lo + ia] <= sg * w[lo + ib];
+    int li = takeA ? ia : ib;
+    if (takeA)
+      ++a;
+    else
+      ++b;
+    perm[t] = li;
+    Ds[t] = sg * w[lo + li];
+    // z: last row of block 1 / first row of block 2 (Q block rows in global coordinates)
+    zs[t] = (li < n1) ? Q[(size_t)(lo + li) * n + (mid - 1)] : Q[(size_t)(lo + li) * n + mid];
+  }
+  double nz = 0.0;
+  for (int t = 0; t < nb; ++t) nz += zs[t] * zs[t];
+  nz = sqrt(nz);
+  rho = rho * nz * nz;
+  double dmax = 0.0;
+  for (int t = 0; t < nb; ++t) {
+    zs[t] /= nz;
+    dmax = fmax(dmax, fabs(Ds[t]));
+  }
+  const double tol = 8.0 * 2.220446049250313e-16 * fmax(dmax, rho);
+  int k = 0, nrot = 0, prev = -1;
+  int* rpq = W.rot_pq + 2 * lo;
+  double* rcs = W.rot_cs + 2 * lo;
+  for (int t = 0; t < nb; ++t) {
+    if (rho * fabs(zs[t]) <= tol) {
+      kind[t] = 0;
+      zs[t] = 0.0;
+      continue;
+    }
+    kind[t] = 1;
+    if (prev >= 0 && fabs(Ds[t] - Ds[prev]) <= tol) {
+      double r = hypot(zs[t], zs[prev]);
+      double c = zs[t] / r, s = zs[prev] / r;
+      double dp = Ds[prev], dt = Ds[t];
+      Ds[prev] = c * c * dp + s * s * dt;
+      Ds[t] = s * s * dp + c * c * dt;
+      zs[prev] = 0.0;
+      zs[t] = r;
+      kind[prev] = 0;
+      rpq[2 * nrot] = perm[prev];
+      rpq[2 * nrot + 1] = perm[t];
+      rcs[2 * nrot] = c;
+      rcs[2 * nrot + 1] = s;
+      ++nrot;
+    }
+    prev = t;
+  }
+  for (int t = 0; t < nb; ++t) k += kind[t];
+  W.rho[mi] = rho;
+  W.counts[3 * mi] = k;
+  W.counts[3 * mi + 1] = nrot;
+  W.counts[3 * mi + 2] = flip;
+}
+
+// Apply the deflation rotations to the block's columns: one thread per row.
+__global__ void merge_rot_kernel(double* Q, int n, const MergeDesc* md, int mi, MergeWork W, int nrot) {
+  const MergeDesc M = md[mi];
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  int nb = M.hi - M.lo;
+  if (r >= nb) return;
+  const int* rpq = W.rot_pq + 2 * M.lo;
+  const double* rcs = W.rot_cs + 2 * M.lo;
+  double* row = Q + (M.lo + r);
+  for (int q = 0; q < nrot; ++q) {
+    size_t cp = (size_t)(M.lo + rpq[2 * q]) * n, ci = (size_t)(M.lo + rpq[2 * q + 1]) * n;
+    double c = rcs[2 * q], s = rcs[2 * q + 1];
+    double xp = row[cp], xi = row[ci];
+    row[cp] = c * xp - s * xi;
+    row[ci] = s * xp + c * xi;
+  }
+}
+
+// Secular roots: thread j of the grid handles root j of the merge.  Dk, zk: the
+// non-deflated poles (ascending) and weights; Delta[i * k + j] = Dk[j] - lambda_i.
+__global__ void secular_kernel(const double* Dk, const double* zk, int k, double rho, double* lam,
+                               double* Delta) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  const double eps = 2.220446049250313e-16;
+  int org;
+  double lo, hi;
+  if (i < k - 1) {
+    double gap = Dk[i + 1] - Dk[i];
+    double mid = Dk[i] + 0.5 * gap;
+    double f = 1.0;
+    for (int j = 0; j < k; ++j) f += rho * zk[j] * zk[j] / (Dk[j] - mid);
+    if (f >= 0) {
+      org = i;
+      lo = 0.0;
+      hi = 0.5 * gap;
+    } else {
+      org = i + 1;
+      lo = -0.5 * gap;
+      hi = 0.0;
+    }
+  } else {
+    org = k - 1;
+    lo = 0.0;
+    hi = rho;
+  }
+  const double dorg = Dk[org];
+  double tau = 0.5 * (lo + hi);
+  for (int it = 0; it < 200; ++it) {
+    double f = 1.0, fp = 0.0, fa = 1.0;
+    for (int j = 0; j < k; ++j) {
+      double del = (Dk[j] - dorg) - tau;
+      double q = zk[j] / del;
+      double term = rho * zk[j] * q;
+      f += term;
+      fa += fabs(term);
+      fp += rho * q * q;
+    }
+    if (f > 0)
+      hi = tau;
+    else
+      lo = tau;
+    if (fabs(f) <= 4.0 * eps * k * fa) break;
+    double tn = tau - f / fp;
+    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
+    if (tn == tau || hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi))) break;
+    tau = tn;
+  }
+  lam[i] = dorg + tau;
+  for (int j = 0; j < k; ++j) Delta[(size_t)i * k + j] = (Dk[j] - dorg) - tau;
+}
+
+// Gu-Eisenstat: zhat_j^2 = (lam_j - D_j)/rho * prod_{i != j} (lam_i - D_j)/(D_i - D_j)
+__global__ void gu_eisenstat_kernel(const double* Dk, const double* zk, int k, double rho, const double* Delta,
+                                    double* zh) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= k) return;
+  double p = -Delta[(size_t)j * k + j] / rho;
+  for (int i = 0; i < k; ++i)
+    if (i != j) p *= (-Delta[(size_t)i * k + j]) / (Dk[i] - Dk[j]);
+  zh[j] = copysign(sqrt(fmax(p, 0.0)), zk[j]);
+}
+
+// S^T (k x k, column-major: column i = normalised eigenvector of root i)
+__global__ void secular_vectors_kernel(const double* zh, int k, const double* Delta, double* St) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  double nrm = 0.0;
+  for (int j = 0; j < k; ++j) {
+    double s = zh[j] / Delta[(size_t)i * k + j];
+    nrm += s * s;
+  }
+  nrm = 1.0 / sqrt(nrm);
+  for (int j = 0; j < k; ++j) St[j + (size_t)i * k] = zh[j] / Delta[(size_t)i * k + j] * nrm;
+}
+
+// Gather the non-deflated (rotated) columns of the block into a contiguous nb x k matrix
+// and their poles / weights into Dk, zk.
+__global__ void gather_nondeflated_kernel(const double* Q, int n, int lo, int nb, const int* perm, const int* kind,
+                                          const double* Ds, const double* zs, int* kpos, double* Qk, double* Dk,
+                                          double* zk) {
+  // kpos: position of each sorted slot among the non-deflated ones (thread 0)
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    int k = 0;
+    for (int t = 0; t < nb; ++t) {
+      kpos[t] = kind[t] ? k : -1;
+      if (kind[t]) {
+        Dk[k] = Ds[t];
+        zk[k] = zs[t];
+        ++k;
+      }
+    }
+  }
+}
+
+__global__ void gather_cols_kernel(const double* Q, int n, int lo, int nb, const int* perm, const int* kpos, double* Qk) {
+  size_t tot = (size_t)nb * nb;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int r = int(e % nb), t = int(e / nb);
+    int kp = kpos[t];
+    if (kp < 0) continue;
+    Qk[r + (size_t)kp * nb] = Q[(size_t)(lo + perm[t]) * n + (lo + r)];
+  }
+}
+
+// Final ordering of the block: eigenvalues = roots (non-deflated) and deflated poles,
+// signs undone, sorted ascending; writes the new block of Q (into Qnew, nb x nb) and w.
+__global__ void merge_finalize_order_kernel(const double* Ds, const int* kind, const double* lam, int nb, int flip,
+                                            int* src_kind, int* src_idx, double* wout) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  // roots (ascending in the flipped space) and deflated poles (ascending) merged
+  int nr = 0, nd = 0;
+  for (int t = 0; t < nb; ++t) {
+    if (kind[t])
+      ++nr;
+    else
+      ++nd;
+  }
+  int ia = 0, ib = 0, pos = 0;
+  int dslot = 0;
+  while (dslot < nb && kind[dslot]) ++dslot;
+  while (ia < nr || ib < nd) {
+    bool takeRoot;
+    if (ia >= nr)
+      takeRoot = false;
+    else if (ib >= nd)
+      takeRoot = true;
+    else
+      takeRoot = lam[ia] <= Ds[dslot];
+    int out = flip ? (nb - 1 - pos) : pos;
+    if (takeRoot) {
+      src_kind[out] = 1;
+      src_idx[out] = ia;
+      wout[out] = flip ? -lam[ia] : lam[ia];
+      ++ia;
+    } else {
+      src_kind[out] = 0;
+      src_idx[out] = dslot;
+      wout[out] = flip ? -Ds[dslot] : Ds[dslot];
+      ++ib;
+      ++dslot;
+      while (dslot < nb && kind[dslot]) ++dslot;
+    }
+    ++pos;
+  }
+}
+
+__global__ void merge_scatter_kernel(const double* Qold, int n, int lo, int nb, const int* perm, const double* Qmerged,
+                                     const int* src_kind, const int* src_idx, double* Qnew) {
+  size_t tot = (size_t)nb * nb;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int r = int(e % nb), out = int(e / nb);
+    double v;
+    if (src_kind[out])
+      v = Qmerged[r + (size_t)src_idx[out] * nb];
+    else
+      v = Qold[(size_t)(lo + perm[src_idx[out]]) * n + (lo + r)];
+    Qnew[r + (size_t)out * nb] = v;
+  }
+}
+
+__global__ void copy_block_kernel(const double* src, int nb, double* Q, int n, int lo, const double* wsrc, double* w) {
+  size_t tot = (size_t)nb * nb;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int r = int(e % nb), cidx = int(e / nb);
+    Q[(size_t)(lo + cidx) * n + (lo + r)] = src[e];
+  }
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)nb; e += (size_t)gridDim.x * blockDim.x)
+    w[lo + e] = wsrc[e];
+}
+
+// complex phases: T's subdiagonal is real by construction except possibly the last one
+__global__ void real_to_complex_kernel(const double* Zr, int64_t rows, int64_t cols, int64_t ldr, double2* Zc,
+                                       int64_t ldc) {
+  size_t tot = (size_t)rows * cols;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int64_t i = e % rows, j = e / rows;
+    Zc[i + j * ldc] = make_double2(Zr[i + j * ldr], 0.0);
+  }
+}
+
+__global__ void scale_rows_phase_kernel(double2* Z, int64_t rows, int64_t cols, int64_t ld, const double2* ph) {
+  size_t tot = (size_t)rows * cols;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int64_t i = e % rows, j = e / rows;
+    double2 z = Z[i + j * ld], p = ph[i];
+    Z[i + j * ld] = make_double2(p.x * z.x - p.y * z.y, p.x * z.y + p.y * z.x);
+  }
+}
+
+// compact WY: T factor (upper triangular, nbk x nbk) for reflectors k0..k0+nbk-1 from
+// S = V^H V (nbk x nbk): T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] S[0:j, j]
+template <typename T>
+__global__ void wy_tfactor_kernel(const T* S, int nbk, const T* tau, T* Tm) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  for (int j = 0; j < nbk; ++j) {
+    T tj = tau[j];
+    for (int i = 0; i < nbk; ++i) Tm[i + j * nbk] = czero<T>();
+    Tm[j + j * nbk] = tj;
+    for (int i = 0; i < j; ++i) {
+      T acc = czero<T>();
+      for (int l = i; l < j; ++l) acc = cadd(acc, cmulv(Tm[i + l * nbk], S[l + j * nbk]));
+      Tm[i + j * nbk] = cscale(cmulv(tj, acc), -1.0);
+    }
+  }
+}
+
+// Extract reflector block V (rows k0+1..n-1, unit diagonal, zeros above) from A.
+template <typename T>
+__global__ void wy_extract_kernel(const T* A, int n, int k0, int nbk, T* V) {
+  int rows = n - (k0 + 1);
+  size_t tot = (size_t)rows * nbk;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    int r = int(e % rows), j = int(e / rows);
+    int gr = k0 + 1 + r, kk = k0 + j;  // reflector kk has v[kk+1] = 1, support rows > kk
+    T val;
+    if (gr < kk + 1)
+      val = czero<T>();
+    else if (gr == kk + 1)
+      val = cone<T>();
+    else
+      val = A[gr + (size_t)kk * n];
+    V[r + (size_t)j * rows] = val;
+  }
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// host orchestration
+// ---------------------------------------------------------------------------
+
+struct DevBuf {
+  nsg_ctx* c;
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf(nsg_ctx* cc, size_t b) : c(cc), bytes(b) { p = dalloc(c, b); }
+  ~DevBuf() { dfree(c, p, bytes); }
+  template <typename T>
+  T* as() {
+    return (T*)p;
+  }
+};
+
+static void build_tree(int lo, int hi, std::vector<std::vector<MergeDesc>>& levels, std::vector<int>& leaf_lo,
+                       std::vector<int>& leaf_hi, int depth) {
+  if (hi - lo <= kLeaf) {
+    leaf_lo.push_back(lo);
+    leaf_hi.push_back(hi);
+    return;
+  }
+  int mid = lo + (hi - lo) / 2;
+  build_tree(lo, mid, levels, leaf_lo, leaf_hi, depth + 1);
+  build_tree(mid, hi, levels, leaf_lo, leaf_hi, depth + 1);
+  if ((int)levels.size() <= depth) levels.resize(depth + 1);
+  levels[depth].push_back(MergeDesc{lo, mid, hi, 0.0});
+}
+
+// Eigen-decomposition of the real symmetric tridiagonal (d, e); Q: n x n (device,
+// column-major), w: eigenvalues ascending (device).
+static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const std::vector<double>& e_in, double* Q,
+                       double* w) {
+  std::vector<std::vector<MergeDesc>> levels;
+  std::vector<int> llo, lhi;
+  build_tree(0, n, levels, llo, lhi, 0);
+  // modified diagonal: for each split subtract beta at the two touching diagonals
+  std::vector<double> d = d_in;
+  for (auto& lv : levels)
+    for (auto& m : lv) {
+      m.beta = e_in[m.mid - 1];
+      d[m.mid - 1] -= m.beta;
+      d[m.mid] -= m.beta;
+    }
+  DevBuf dd(c, sizeof(double) * n), de(c, sizeof(double) * std::max(n, 1));
+  NSG_CUDA(cudaMemcpyAsync(dd.p, d.data(), sizeof(double) * n, cudaMemcpyHostToDevice, c->stream));
+  NSG_CUDA(cudaMemcpyAsync(de.p, e_in.data(), sizeof(double) * std::max<size_t>(e_in.size(), 1),
+                           cudaMemcpyHostToDevice, c->stream));
+  NSG_CUDA(cudaMemsetAsync(Q, 0, sizeof(double) * n * n, c->stream));
+  // leaves
+  int nleaf = int(llo.size());
+  DevBuf dlo(c, sizeof(int) * nleaf), dhi(c, sizeof(int) * nleaf);
+  NSG_CUDA(cudaMemcpyAsync(dlo.p, llo.data(), sizeof(int) * nleaf, cudaMemcpyHostToDevice, c->stream));
+  NSG_CUDA(cudaMemcpyAsync(dhi.p, lhi.data(), sizeof(int) * nleaf, cudaMemcpyHostToDevice, c->stream));
+  DevBuf LM(c, sizeof(double) * nleaf * kLeaf * kLeaf), LV(c, sizeof(double) * nleaf * kLeaf * kLeaf),
+      LW(c, sizeof(double) * nleaf * kLeaf);
+  leaf_build_kernel<<<nleaf, 256, 0, c->stream>>>(dd.as<double>(), de.as<double>(), dlo.as<int>(), dhi.as<int>(),
+                                                  nleaf, LM.as<double>());
+  count_launch(c);
+  jacobi_batched(c, kLeaf, nleaf, LM.as<double>(), LV.as<double>(), LW.as<double>());
+  leaf_scatter_kernel<<<nleaf, 256, 0, c->stream>>>(LM.as<double>(), LV.as<double>(), LW.as<double>(), dlo.as<int>(),
+                                                    dhi.as<int>(), nleaf, Q, n, w);
+  count_launch(c);
+  check_launch("dc leaves");
+  // merges, deepest level first
+  MergeWork W;
+  DevBuf bDs(c, sizeof(double) * n), bzs(c, sizeof(double) * n), bperm(c, sizeof(int) * n), bkind(c, sizeof(int) * n),
+      brpq(c, sizeof(int) * 2 * n), brcs(c, sizeof(double) * 2 * n);
+  W.Ds = bDs.as<double>();
+  W.zs = bzs.as<double>();
+  W.perm = bperm.as<int>();
+  W.kind = bkind.as<int>();
+  W.rot_pq = brpq.as<int>();
+  W.rot_cs = brcs.as<double>();
+  for (int L = int(levels.size()) - 1; L >= 0; --L) {
+    auto& lv = levels[L];
+    int nm = int(lv.size());
+    DevBuf bmd(c, sizeof(MergeDesc) * nm), brho(c, sizeof(double) * nm), bcnt(c, sizeof(int) * 3 * nm);
+    W.rho = brho.as<double>();
+    W.counts = bcnt.as<int>();
+    NSG_CUDA(cudaMemcpyAsync(bmd.p, lv.data(), sizeof(MergeDesc) * nm, cudaMemcpyHostToDevice, c->stream));
+    merge_prep_kernel<<<nm, 32, 0, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
+    count_launch(c);
+    check_launch("dc prep");
+    std::vector<double> rho(nm);
+    std::vector<int> cnt(3 * nm);
+    NSG_CUDA(cudaMemcpyAsync(rho.data(), brho.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(cnt.data(), bcnt.p, sizeof(int) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaStreamSynchronize(c->stream));
+    for (int mi = 0; mi < nm; ++mi) {
+      const MergeDesc& M = lv[mi];
+      int nb = M.hi - M.lo, k = cnt[3 * mi], nrot = cnt[3 * mi + 1], flip = cnt[3 * mi + 2];
+      if (nrot > 0) {
+        merge_rot_kernel<<<(nb + 127) / 128, 128, 0, c->stream>>>(Q, n, bmd.as<MergeDesc>(), mi, W, nrot);
+        count_launch(c);
+      }
+      DevBuf Dk(c, sizeof(double) * std::max(k, 1)), zk(c, sizeof(double) * std::max(k, 1)),
+          kpos(c, sizeof(int) * nb), lam(c, sizeof(double) * std::max(k, 1));
+      DevBuf Qk(c, sizeof(double) * (size_t)nb * std::max(k, 1)), Qm(c, sizeof(double) * (size_t)nb * std::max(k, 1));
+      gather_nondeflated_kernel<<<1, 32, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, W.kind + M.lo, W.Ds + M.lo,
+                                                         W.zs + M.lo, kpos.as<int>(), Qk.as<double>(), Dk.as<double>(),
+                                                         zk.as<double>());
+      int gblocks = int(std::min<size_t>(((size_t)nb * nb + 255) / 256, (size_t)c->num_sms * 8));
+      gather_cols_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, kpos.as<int>(),
+                                                         Qk.as<double>());
+      count_launch(c, 2);
+      if (k > 0) {
+        DevBuf Delta(c, sizeof(double) * (size_t)k * k), zh(c, sizeof(double) * k),
+            St(c, sizeof(double) * (size_t)k * k);
+        int tb = 64, gb = (k + tb - 1) / tb;
+        secular_kernel<<<gb, tb, 0, c->stream>>>(Dk.as<double>(), zk.as<double>(), k, rho[mi], lam.as<double>(),
+                                                 Delta.as<double>());
+        gu_eisenstat_kernel<<<gb, tb, 0, c->stream>>>(Dk.as<double>(), zk.as<double>(), k, rho[mi],
+                                                      Delta.as<double>(), zh.as<double>());
+        secular_vectors_kernel<<<gb, tb, 0, c->stream>>>(zh.as<double>(), k, Delta.as<double>(), St.as<double>());
+        count_launch(c, 3);
+        check_launch("dc secular");
+        GemmArgs g;
+        g.dtype = NSG_F64;
+        g.M = nb;
+        g.N = k;
+        g.K = k;
+        g.A = Qk.p;
+        g.lda = nb;
+        g.opA = OP_N;
+        g.B = St.p;
+        g.ldb = k;
+        g.opB = OP_N;
+        g.C = Qm.p;
+        g.ldc = nb;
+        g.batch = 1;
+        g.strideA = g.strideB = g.strideC = 0;
+        gemm_f64_simt(c, g);
+      }
+      DevBuf skind(c, sizeof(int) * nb), sidx(c, sizeof(int) * nb), wnew(c, sizeof(double) * nb),
+          Qnew(c, sizeof(double) * (size_t)nb * nb);
+      merge_finalize_order_kernel<<<1, 32, 0, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(), nb, flip,
+                                                           skind.as<int>(), sidx.as<int>(), wnew.as<double>());
+      merge_scatter_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, Qm.as<double>(),
+                                                           skind.as<int>(), sidx.as<int>(), Qnew.as<double>());
+      copy_block_kernel<<<gblocks, 256, 0, c->stream>>>(Qnew.as<double>(), nb, Q, n, M.lo, wnew.as<double>(), w);
+      count_launch(c, 3);
+      check_launch("dc merge");
+    }
+  }
+}
+
+template <typename T>
+static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* tau_dev, T* Z, int64_t ldz, int64_t k) {
+  // Z <- H_0 H_1 ... H_{n-3} Z, blocks of 32 reflectors applied last block first
+  const int nref = n - 2;
+  if (nref <= 0 || k == 0) return;
+  const int NB = 32;
+  const size_t eb = sizeof(T);
+  DevBuf V(c, eb * (size_t)n * NB), S(c, eb * NB * NB), Tm(c, eb * NB * NB), Wt(c, eb * (size_t)NB * k),
+      W2(c, eb * (size_t)NB * k);
+  for (int k0 = ((nref - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
+    int nbk = std::min(NB, nref - k0);
+    int rows = n - (k0 + 1);
+    int gblocks = int(std::min<size_t>(((size_t)rows * nbk + 255) / 256, (size_t)c->num_sms * 8));
+    wy_extract_kernel<T><<<gblocks, 256, 0, c->stream>>>(A, n, k0, nbk, V.as<T>());
+    count_launch(c);
+    // S = V^H V
+    GemmArgs g;
+    g.dtype = dtype;
+    g.batch = 1;
+    g.strideA = g.strideB = g.strideC = 0;
+    g.M = nbk;
+    g.N = nbk;
+    g.K = rows;
+    g.A = V.p;
+    g.lda = rows;
+    g.opA = OP_C;
+    g.B = V.p;
+    g.ldb = rows;
+    g.opB = OP_N;
+    g.C = S.p;
+    g.ldc = nbk;
+    gemm_f64_simt(c, g);
+    wy_tfactor_kernel<T><<<1, 32, 0, c->stream>>>(S.as<T>(), nbk, tau_dev + k0, Tm.as<T>());
+    count_launch(c);
+    // W = V^H Z(rows k0+1..)  (nbk x k)
+    GemmArgs h = g;
+    h.M = nbk;
+    h.N = k;
+    h.K = rows;
+    h.A = V.p;
+    h.lda = rows;
+    h.opA = OP_C;
+    h.B = Z + (k0 + 1);
+    h.ldb = ldz;
+    h.opB = OP_N;
+    h.C = Wt.p;
+    h.ldc = nbk;
+    gemm_f64_simt(c, h);
+    // W2 = T W
+    GemmArgs t2 = g;
+    t2.M = nbk;
+    t2.N = k;
+    t2.K = nbk;
+    t2.A = Tm.p;
+    t2.lda = nbk;
+    t2.opA = OP_N;
+    t2.B = Wt.p;
+    t2.ldb = nbk;
+    t2.opB = OP_N;
+    t2.C = W2.p;
+    t2.ldc = nbk;
+    gemm_f64_simt(c, t2);
+    // Z -= V W2
+    GemmArgs u = g;
+    u.M = rows;
+    u.N = k;
+    u.K = nbk;
+    u.A = V.p;
+    u.lda = rows;
+    u.opA = OP_N;
+    u.B = W2.p;
+    u.ldb = nbk;
+    u.opB = OP_N;
+    u.C = Z + (k0 + 1);
+    u.ldc = ldz;
+    u.alpha_re = -1.0;
+    u.beta_re = 1.0;
+    gemm_f64_simt(c, u);
+  }
+  check_launch("back_transform");
+}
+
+// Hermitian eigen-decomposition of A (n x n, consumed).  Eigenvalues ascending into
+// w_host; eigenvectors for the eigenvalue indices `cols` (ascending order indices)
+// into Zout (n x ncols, column-major).  The caller chooses cols after seeing the
+// spectrum through `pick`.
+template <typename T>
+static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double>& w_host, const PickFn& pick) {
+  const size_t eb = sizeof(T);
+  DevBuf dd(c, sizeof(double) * n), de(c, sizeof(double) * std::max(n, 1)), dtau(c, eb * std::max(n, 1));
+  NSG_CUDA(cudaMemsetAsync(dtau.p, 0, eb * std::max(n, 1), c->stream));
+  std::vector<double> d(n), e(std::max(n - 1, 0));
+  if (n == 1) {
+    T a;
+    NSG_CUDA(cudaMemcpyAsync(&a, A, eb, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaStreamSynchronize(c->stream));
+    d[0] = ((double*)&a)[0];
+  } else {
+    // cooperative tridiagonalisation
+    int max_blocks = 0;
+    size_t shm = eb * n;
+    if (shm > 48 * 1024)
+      NSG_CUDA(cudaFuncSetAttribute(tridiag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    NSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks, tridiag_kernel<T>, kTriThreads, shm));
+    NSG_CHECK(max_blocks > 0, NSG_ERR_UNSUPPORTED, "tridiagonalisation: no resident block fits");
+    int64_t want = ((int64_t)n * n + kTriThreads * 8 - 1) / (kTriThreads * 8);
+    int grid = int(std::min<int64_t>({(int64_t)max_blocks * c->num_sms, std::max<int64_t>(want, 1),
+                                      (int64_t)c->num_sms * 2}));
+    DevBuf xbuf(c, eb * n), part(c, sizeof(double2) * grid), bar(c, sizeof(Barrier));
+    NSG_CUDA(cudaMemsetAsync(bar.p, 0, sizeof(Barrier), c->stream));
+    double* pd = dd.as<double>();
+    double* pe = de.as<double>();
+    T* pt = dtau.as<T>();
+    T* px = xbuf.as<T>();
+    T* pp = part.as<T>();
+    Barrier* pb = bar.as<Barrier>();
+    void* args[] = {&A, &n, &pd, &pe, &pt, &px, &pp, &pb};
+    NSG_CUDA(cudaLaunchCooperativeKernel((void*)tridiag_kernel<T>, dim3(grid), dim3(kTriThreads), args, shm,
+                                         c->stream));
+    count_launch(c);
+    check_launch("tridiag");
+    Barrier hb;
+    NSG_CUDA(cudaMemcpyAsync(&hb, bar.p, sizeof(Barrier), cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(d.data(), dd.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(e.data(), de.p, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaStreamSynchronize(c->stream));
+    NSG_CHECK(hb.err == 0, NSG_ERR_TIMEOUT, "tridiagonalisation: grid barrier timed out");
+  }
+  std::vector<double2> phase(n, make_double2(1.0, 0.0));
+  if constexpr (sizeof(T) == 16) {
+    // the last subdiagonal entry A[n-1, n-2] may be complex: make it real with a phase on row n-1
+    if (n >= 2) {
+      double2 last;
+      NSG_CUDA(cudaMemcpyAsync(&last, (double2*)A + (n - 1) + (size_t)(n - 2) * n, sizeof(double2),
+                               cudaMemcpyDeviceToHost, c->stream));
+      NSG_CUDA(cudaStreamSynchronize(c->stream));
+      double r = std::hypot(last.x, last.y);
+      e[n - 2] = r;
+      if (r > 0) phase[n - 1] = make_double2(last.x / r, last.y / r);
+    }
+  }
+  for (double x : d) NSG_CHECK(std::isfinite(x), NSG_ERR_NONFINITE, "eigensolver: non-finite tridiagonal");
+  for (double x : e) NSG_CHECK(std::isfinite(x), NSG_ERR_NONFINITE, "eigensolver: non-finite tridiagonal");
+  DevBuf Q(c, sizeof(double) * (size_t)n * n), wdev(c, sizeof(double) * n);
+  if (n == 1) {
+    double one = 1.0;
+    NSG_CUDA(cudaMemcpyAsync(Q.p, &one, sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(wdev.p, d.data(), sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  } else {
+    tridiag_dc(c, n, d, e, Q.as<double>(), wdev.as<double>());
+  }
+  w_host.resize(n);
+  NSG_CUDA(cudaMemcpyAsync(w_host.data(), wdev.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  for (double x : w_host) NSG_CHECK(std::isfinite(x), NSG_ERR_NONFINITE, "eigensolver: non-finite eigenvalue");
+  void* Zv = nullptr;
+  int64_t ldz = 0;
+  std::vector<int> cols = pick(w_host, &Zv, &ldz);
+  T* Zout = (T*)Zv;
+  int64_t kc = int64_t(cols.size());
+  if (kc == 0) return;
+  // gather the chosen tridiagonal eigenvectors into Zout (real -> T)
+  DevBuf didx(c, sizeof(int) * kc);
+  NSG_CUDA(cudaMemcpyAsync(didx.p, cols.data(), sizeof(int) * kc, cudaMemcpyHostToDevice, c->stream));
+  if constexpr (sizeof(T) == 8) {
+    copy_columns(c, NSG_F64, n, kc, Q.p, n, didx.as<int>(), Zout, ldz);
+  } else {
+    DevBuf Zr(c, sizeof(double) * (size_t)n * kc);
+    copy_columns(c, NSG_F64, n, kc, Q.p, n, didx.as<int>(), Zr.p, n);
+    int gblocks = int(std::min<size_t>(((size_t)n * kc + 255) / 256, (size_t)c->num_sms * 8));
+    real_to_complex_kernel<<<gblocks, 256, 0, c->stream>>>(Zr.as<double>(), n, kc, n, (double2*)Zout, ldz);
+    DevBuf ph(c, sizeof(double2) * n);
+    NSG_CUDA(cudaMemcpyAsync(ph.p, phase.data(), sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+    scale_rows_phase_kernel<<<gblocks, 256, 0, c->stream>>>((double2*)Zout, n, kc, ldz, ph.as<double2>());
+    count_launch(c, 2);
+  }
+  back_transform<T>(c, dtype, n, A, dtau.as<T>(), Zout, ldz, kc);
+}
+
+void syevd_dc(nsg_ctx* c, int dtype, int n, void* A, std::vector<double>& w_host, const PickFn& pick) {
+  if (dtype == NSG_C128)
+    syevd_dc_impl<double2>(c, dtype, n, (double2*)A, w_host, pick);
+  else
+    syevd_dc_impl<double>(c, dtype, n, (double*)A, w_host, pick);
+}
+
+}  // namespace nsg

@@ -252,3 +252,33 @@ def test_errors_are_reported(nsg_ctx):
     T = DTensor.from_numpy(np.ones((3, 4)), [a, b])
     with pytest.raises(NsgError):
         it.factorize(T, [], cutoff=0.0)
+
+
+def _dmrg_like(rng, m, n, cplx):
+    """Singular values with exact triple degeneracies and a long tail (an SU(2)-like
+    entanglement spectrum), as the Gram matrices of a DMRG bond have."""
+    k = min(m, n)
+    s = np.repeat(np.exp(-0.12 * np.arange((k + 2) // 3)), 3)[:k]
+    s[2 * k // 3:] *= 1e-7
+    U, _ = np.linalg.qr(rnd(rng, (m, k), cplx))
+    V, _ = np.linalg.qr(rnd(rng, (n, k), cplx))
+    return (U * s) @ V.conj().T
+
+
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("m,n", [(1, 3), (33, 33), (64, 40), (200, 260), (513, 513), (1100, 900)])
+def test_eigensolver_large_and_degenerate(nsg_ctx, cplx, m, n):
+    rng = np.random.default_rng(m + 7 * n)
+    M = _dmrg_like(rng, m, n, cplx)
+    l, r = Index(m), Index(n)
+    T = DTensor.from_numpy(M, [l, r])
+    for cutoff, maxdim in [(0.0, None), (1e-12, None), (1e-8, 3 * min(m, n) // 4 + 1)]:
+        U, Cc, info = it.factorize(T, [l], cutoff=cutoff, maxdim=maxdim, spectrum=True)
+        s = np.linalg.svd(M, compute_uv=False)
+        kref, errref = ol.truncate_spectrum(s ** 2, cutoff, maxdim)
+        assert info["newdim"] == kref, (cutoff, maxdim)
+        u = U.to_numpy().reshape(m, -1)
+        assert np.abs(u.conj().T @ u - np.eye(kref)).max() < 1e-12
+        Pk = u @ Cc.to_numpy().reshape(kref, n)
+        assert abs(np.linalg.norm(M - Pk) ** 2 / np.linalg.norm(M) ** 2 - errref) < 1e-12
+        assert rel(info["spectrum"][:kref], s[:kref] ** 2) < 1e-12
