@@ -7,6 +7,8 @@
 // touch consecutive addresses for either operand orientation.
 #include "nsg_internal.h"
 
+#include <algorithm>
+
 namespace nsg {
 
 namespace {
@@ -48,21 +50,28 @@ struct Scal<double2> {
   }
 };
 
+// splits > 1: grid z covers batch * splits; split sp sums k in [sp*ksplit, (sp+1)*ksplit)
+// and writes its raw partial product to C + bz * M * N (ld = M); a reduction applies
+// alpha / beta afterwards in a fixed order.
 template <typename T, int BK>
 __global__ void __launch_bounds__(NT)
-    gemm_kernel(int64_t M, int64_t N, int64_t K, const T* __restrict__ A, int64_t lda, int64_t sA, int opA,
+    gemm_kernel(int64_t M, int64_t N, int64_t Kfull, const T* __restrict__ A, int64_t lda, int64_t sA, int opA,
                 const T* __restrict__ B, int64_t ldb, int64_t sB, int opB, T* __restrict__ C, int64_t ldc,
-                int64_t sC, int64_t batch, Scal<T> sc) {
+                int64_t sC, int64_t batch, Scal<T> sc, int splits, int64_t ksplit) {
   __shared__ T As[BK][BM + 1];
   __shared__ T Bs[BK][BN + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t m0 = int64_t(blockIdx.x) * BM, n0 = int64_t(blockIdx.y) * BN;
   const bool transA = (opA == OP_T || opA == OP_C), conjA = (opA == OP_C || opA == OP_R);
   const bool transB = (opB == OP_T || opB == OP_C), conjB = (opB == OP_C || opB == OP_R);
-  for (int64_t bz = blockIdx.z; bz < batch; bz += gridDim.z) {
-    const T* Ab = A + bz * sA;
-    const T* Bb = B + bz * sB;
-    T* Cb = C + bz * sC;
+  for (int64_t bzz = blockIdx.z; bzz < batch * splits; bzz += gridDim.z) {
+    const int64_t bz = bzz / splits, sp = bzz % splits;
+    const int64_t kb = sp * ksplit;
+    const int64_t K = (splits > 1) ? ((kb + ksplit < Kfull) ? ksplit : Kfull - kb) : Kfull;
+    const T* Ab = A + bz * sA + (transA ? kb : kb * lda);
+    const T* Bb = B + bz * sB + (transB ? kb * ldb : kb);
+    T* Cb = (splits > 1) ? C + bzz * M * N : C + bz * sC;
+    const int64_t ldcc = (splits > 1) ? M : ldc;
     T acc[4][4];
 #pragma unroll
     for (int i = 0; i < 4; ++i)
@@ -128,10 +137,35 @@ __global__ void __launch_bounds__(NT)
       for (int j = 0; j < 4; ++j) {
         int64_t gj = n0 + tx + 16 * j;
         if (gj >= N) continue;
-        T* cp = Cb + gi + gj * ldc;
-        *cp = sc.epi(acc[i][j], cp);
+        T* cp = Cb + gi + gj * ldcc;
+        if (splits > 1)
+          *cp = acc[i][j];
+        else
+          *cp = sc.epi(acc[i][j], cp);
       }
     }
+  }
+}
+
+template <typename T>
+__global__ void splitk_reduce_kernel(int64_t M, int64_t N, int64_t batch, int splits, const T* __restrict__ W,
+                                     T* __restrict__ C, int64_t ldc, int64_t sC, Scal<T> sc) {
+  const int64_t MN = M * N, tot = MN * batch;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+    int64_t b = e / MN, r = e % MN, i = r % M, j = r / M;
+    T acc;
+    zero(acc);
+    for (int sp = 0; sp < splits; ++sp) {
+      T v = W[(b * splits + sp) * MN + r];
+      if constexpr (sizeof(T) == 8) {
+        acc += v;
+      } else {
+        acc.x += v.x;
+        acc.y += v.y;
+      }
+    }
+    T* cp = C + b * sC + i + j * ldc;
+    *cp = sc.epi(acc, cp);
   }
 }
 
@@ -141,19 +175,58 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   if (g.M == 0 || g.N == 0 || g.batch == 0) return;
   int64_t gx = (g.M + BM - 1) / BM, gy = (g.N + BN - 1) / BN;
   NSG_CHECK(gx < (1ll << 31) && gy < 65536, NSG_ERR_UNSUPPORTED, "gemm: grid too large");
-  int64_t gz = g.batch < 65535 ? g.batch : 65535;
+  // split K when the tile grid cannot fill the GPU
+  int splits = 1;
+  int64_t ksplit = g.K;
+  const int64_t tiles = gx * gy * g.batch;
+  const int64_t sms = c->num_sms > 0 ? c->num_sms : 152;
+  if (tiles < sms && g.K >= 512) {
+    int64_t want = (2 * sms + tiles - 1) / tiles;
+    int64_t maxs = g.K / 256;
+    splits = int(std::min<int64_t>({want, maxs, 64}));
+    if (splits < 2) splits = 1;
+    ksplit = (g.K + splits - 1) / splits;
+    ksplit = ((ksplit + 15) / 16) * 16;
+    splits = int((g.K + ksplit - 1) / ksplit);
+  }
+  int64_t zt = g.batch * splits;
+  int64_t gz = zt < 65535 ? zt : 65535;
   dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
+  const size_t eb = g.dtype == NSG_C128 ? 16 : 8;
+  void* W = nullptr;
+  size_t wbytes = 0;
+  void* Cout = g.C;
+  if (splits > 1) {
+    wbytes = eb * size_t(g.M) * size_t(g.N) * size_t(zt);
+    W = dalloc(c, wbytes);
+    Cout = W;
+  }
   if (g.dtype == NSG_C128) {
     Scal<double2> sc{make_double2(g.alpha_re, g.alpha_im), make_double2(g.beta_re, g.beta_im)};
     gemm_kernel<double2, 8><<<grid, NT, 0, c->stream>>>(g.M, g.N, g.K, (const double2*)g.A, g.lda, g.strideA, g.opA,
                                                         (const double2*)g.B, g.ldb, g.strideB, g.opB,
-                                                        (double2*)g.C, g.ldc, g.strideC, g.batch, sc);
+                                                        (double2*)Cout, g.ldc, g.strideC, g.batch, sc, splits, ksplit);
+    if (splits > 1) {
+      int64_t tot = g.M * g.N * g.batch;
+      int rb = int(std::min<int64_t>((tot + 255) / 256, sms * 8));
+      splitk_reduce_kernel<double2><<<rb, 256, 0, c->stream>>>(g.M, g.N, g.batch, splits, (const double2*)W,
+                                                              (double2*)g.C, g.ldc, g.strideC, sc);
+      count_launch(c);
+    }
   } else {
     Scal<double> sc{g.alpha_re, g.beta_re};
     gemm_kernel<double, 16><<<grid, NT, 0, c->stream>>>(g.M, g.N, g.K, (const double*)g.A, g.lda, g.strideA, g.opA,
-                                                        (const double*)g.B, g.ldb, g.strideB, g.opB, (double*)g.C,
-                                                        g.ldc, g.strideC, g.batch, sc);
+                                                        (const double*)g.B, g.ldb, g.strideB, g.opB, (double*)Cout,
+                                                        g.ldc, g.strideC, g.batch, sc, splits, ksplit);
+    if (splits > 1) {
+      int64_t tot = g.M * g.N * g.batch;
+      int rb = int(std::min<int64_t>((tot + 255) / 256, sms * 8));
+      splitk_reduce_kernel<double><<<rb, 256, 0, c->stream>>>(g.M, g.N, g.batch, splits, (const double*)W,
+                                                             (double*)g.C, g.ldc, g.strideC, sc);
+      count_launch(c);
+    }
   }
+  if (W) dfree(c, W, wbytes);
   count_launch(c);
   check_launch("gemm_f64_simt");
 }

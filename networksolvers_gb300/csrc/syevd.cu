@@ -118,70 +118,114 @@ __device__ T block_sum(T v, T* red) {
 }
 
 // Householder tridiagonalisation of the Hermitian n x n matrix A (column-major, both
-// triangles stored).  On exit d[k] = T_kk, e[k] = T_k,k+1 (real), tau[k], and the
-// reflector vectors v_k (v_k[k+1] = 1 implicit) below the subdiagonal of column k.
-// Update per column: x = tau A22 v, w = x - tau/2 (x^H v) v, A22 -= v w^H + w v^H.
+// triangles stored).  On exit d[k] = T_kk, e[k] = T_k,k+1 (real), tau[k], the reflector
+// vectors v_k (v_k[k+1] = 1 implicit) below the subdiagonal of column k, and
+// A[n-1, n-2] updated (its phase is handled by the caller for complex A).
+// Step k: reflector from column k; x = tau A22 v; w = x - tau/2 (x^H v) v;
+// A22 -= v w^H + w v^H.  The rank-2 update of step k-1 is applied lazily: every CTA
+// rebuilds the updated pivot column itself, and one pass over the trailing block both
+// applies the pending update and forms step k's x (one grid barrier per column).  CTAs
+// retire as the trailing block shrinks (the barrier target follows the active count).
 template <typename T>
 __global__ void __launch_bounds__(kTriThreads)
     tridiag_kernel(T* __restrict__ A, int n, double* __restrict__ d, double* __restrict__ e, T* __restrict__ tau,
                    T* __restrict__ xbuf, T* __restrict__ partial, Barrier* bar) {
   extern __shared__ unsigned char smem_raw[];
-  T* v = (T*)smem_raw;  // n entries
+  T* vprev = (T*)smem_raw;  // pending update (relative to rows >= k)
+  T* wprev = vprev + n;
+  T* vcur = wprev + n;      // current reflector (relative to rows >= k+1)
   __shared__ T red[kTriThreads / 32];
-  const int tid = threadIdx.x, nt = blockDim.x, nb = gridDim.x, b = blockIdx.x;
-  const int gtid = b * nt + tid, gnt = nb * nt;
+  __shared__ double2 wsum[kTriThreads / 32];
+  const int tid = threadIdx.x, nt = blockDim.x, b = blockIdx.x;
   const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
-  const int gwarp = b * nwarps + warp, gnwarps = nb * nwarps;
+  bool has_prev = false;
   for (int k = 0; k < n - 2; ++k) {
-    const int m = n - k - 1;  // active size (rows k+1..n-1)
-    T* col = A + (size_t)k * n;
-    // every CTA reads column k and forms the reflector redundantly (same order -> same bits)
+    const int m = n - k - 1;  // trailing size (rows k+1..n-1)
+    int nact = int(((int64_t)m * m + (int64_t)nt * 64 - 1) / ((int64_t)nt * 64));
+    nact = max(1, min(nact, (int)gridDim.x));
+    if (b >= nact) return;
+    const int gwarp = b * nwarps + warp, gnwarps = nact * nwarps;
+    // x and the partial sums are double-buffered by step parity: a CTA that runs ahead
+    // writes the other buffer while a slower one still reads this step's values (the
+    // barrier keeps every CTA within one step of the others)
+    T* xb = xbuf + (size_t)(k & 1) * n;
+    double2* pb = (double2*)partial + (size_t)(k & 1) * gridDim.x;
+    // 1. pivot column k with the pending update applied (rows k..n-1), reflector
+    const T* colk = A + (size_t)k * n;
+    const T wp0 = has_prev ? cconj(wprev[0]) : czero<T>();
+    const T vp0 = has_prev ? cconj(vprev[0]) : czero<T>();
+    auto colval = [&](int i) -> T {  // i >= k
+      T a = colk[i];
+      if (has_prev) a = csub(a, cadd(cmulv(vprev[i - k], wp0), cmulv(wprev[i - k], vp0)));
+      return a;
+    };
     double ss = 0.0;
-    for (int i = k + 2 + tid; i < n; i += nt) ss += cabs2(col[i]);
-    double xnorm2 = block_sum<double>(ss, (double*)red);
-    T alpha = col[k + 1];
-    double ar = cre(alpha);
+    for (int i = k + 2 + tid; i < n; i += nt) ss += cabs2(colval(i));
+    const double xnorm2 = block_sum<double>(ss, (double*)red);
+    const T alpha = colval(k + 1);
+    const double ar = cre(alpha);
     double ai = 0.0;
     if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
     T tk = czero<T>();
     double beta = ar;
     T scale = czero<T>();
-    bool active = !(xnorm2 == 0.0 && ai == 0.0);
+    const bool active = !(xnorm2 == 0.0 && ai == 0.0);
     if (active) {
       double nrm = sqrt(ar * ar + ai * ai + xnorm2);
       beta = ar >= 0 ? -nrm : nrm;
       if constexpr (sizeof(T) == 16) {
         double2 t2 = make_double2((beta - ar) / beta, -ai / beta);
         tk = *(T*)&t2;
-        double2 am = make_double2(ar - beta, ai);
-        double2 inv = cdiv(make_double2(1.0, 0.0), am);
+        double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
         scale = *(T*)&inv;
       } else {
-        double t1 = (beta - ar) / beta;
+        double t1 = (beta - ar) / beta, s1 = 1.0 / (ar - beta);
         tk = *(T*)&t1;
-        double s1 = 1.0 / (ar - beta);
         scale = *(T*)&s1;
       }
     }
-    // v in shared memory (indices 0..m-1 <-> rows k+1..n-1)
-    for (int i = tid; i < m; i += nt) v[i] = (i == 0) ? cone<T>() : cmulv(col[k + 1 + i], scale);
+    for (int r = tid; r < m; r += nt) vcur[r] = (r == 0) ? cone<T>() : cmulv(colval(k + 1 + r), scale);
     __syncthreads();
     if (b == 0 && tid == 0) {
-      d[k] = cre(A[k + (size_t)k * n]);
+      d[k] = cre(colval(k));
       e[k] = active ? beta : ar;
       tau[k] = tk;
     }
-    if (!active) {
-      // H = I; keep column k as is (e[k] = Re(alpha), alpha real) and move on
-      if (!grid_sync(bar)) return;
-      continue;
-    }
-    // x = tau * A22 * v   (row i of A22 = conj(column i) by symmetry: coalesced column reads)
+    // 2. one pass over the trailing block: pending update, then x_j = tau * A22[:, j]^H v
     double2 pacc = make_double2(0.0, 0.0);
-    for (int i = gwarp; i < m; i += gnwarps) {
-      const T* ci = A + (size_t)(k + 1 + i) * n + (k + 1);
-      T acc = czero<T>();
-      for (int j = lane; j < m; j += 32) acc = cadd(acc, cmulv(cconj(ci[j]), v[j]));
+    for (int jj = gwarp; jj < m; jj += gnwarps) {
+      T* cj = A + (size_t)(k + 1 + jj) * n + (k + 1);
+      const T wj = has_prev ? cconj(wprev[jj + 1]) : czero<T>();
+      const T vj = has_prev ? cconj(vprev[jj + 1]) : czero<T>();
+      // four independent loads in flight per lane (the pass is L2-latency bound)
+      T acc = czero<T>(), acc1 = czero<T>(), acc2 = czero<T>(), acc3 = czero<T>();
+      int ii = lane;
+      for (; ii + 96 < m; ii += 128) {
+        T v0 = cj[ii], v1 = cj[ii + 32], v2 = cj[ii + 64], v3 = cj[ii + 96];
+        if (has_prev) {
+          v0 = csub(v0, cadd(cmulv(vprev[ii + 1], wj), cmulv(wprev[ii + 1], vj)));
+          v1 = csub(v1, cadd(cmulv(vprev[ii + 33], wj), cmulv(wprev[ii + 33], vj)));
+          v2 = csub(v2, cadd(cmulv(vprev[ii + 65], wj), cmulv(wprev[ii + 65], vj)));
+          v3 = csub(v3, cadd(cmulv(vprev[ii + 97], wj), cmulv(wprev[ii + 97], vj)));
+          cj[ii] = v0;
+          cj[ii + 32] = v1;
+          cj[ii + 64] = v2;
+          cj[ii + 96] = v3;
+        }
+        acc = cadd(acc, cmulv(cconj(v0), vcur[ii]));
+        acc1 = cadd(acc1, cmulv(cconj(v1), vcur[ii + 32]));
+        acc2 = cadd(acc2, cmulv(cconj(v2), vcur[ii + 64]));
+        acc3 = cadd(acc3, cmulv(cconj(v3), vcur[ii + 96]));
+      }
+      for (; ii < m; ii += 32) {
+        T val = cj[ii];
+        if (has_prev) {
+          val = csub(val, cadd(cmulv(vprev[ii + 1], wj), cmulv(wprev[ii + 1], vj)));
+          cj[ii] = val;
+        }
+        acc = cadd(acc, cmulv(cconj(val), vcur[ii]));
+      }
+      acc = cadd(cadd(acc, acc1), cadd(acc2, acc3));
       for (int o = 16; o > 0; o >>= 1) {
         if constexpr (sizeof(T) == 8) {
           acc += __shfl_down_sync(0xffffffffu, acc, o);
@@ -194,9 +238,8 @@ __global__ void __launch_bounds__(kTriThreads)
       }
       if (lane == 0) {
         T xi = cmulv(tk, acc);
-        xbuf[i] = xi;
-        // accumulate x^H v
-        T p = cmulv(cconj(xi), v[i]);
+        xb[jj] = xi;
+        T p = cmulv(cconj(xi), vcur[jj]);
         if constexpr (sizeof(T) == 8) {
           pacc.x += (double&)p;
         } else {
@@ -205,26 +248,51 @@ __global__ void __launch_bounds__(kTriThreads)
         }
       }
     }
-    // per-CTA partial of x^H v in fixed order: per-warp slot, then CTA sum
-    __shared__ double2 wsum[kTriThreads / 32];
     if (lane == 0) wsum[warp] = pacc;
     __syncthreads();
     if (tid == 0) {
-      double2 s = make_double2(0.0, 0.0);
+      double2 sacc = make_double2(0.0, 0.0);
       for (int w = 0; w < nwarps; ++w) {
-        s.x += wsum[w].x;
-        s.y += wsum[w].y;
+        sacc.x += wsum[w].x;
+        sacc.y += wsum[w].y;
       }
-      ((double2*)partial)[b] = s;
+      pb[b] = sacc;
     }
-    if (!grid_sync(bar)) return;
-    // x^H v: every CTA sums the partials in the same order
+    // 3. barrier among the active CTAs
+    {
+      __shared__ int s_ok;
+      __syncthreads();
+      if (tid == 0) {
+        volatile unsigned int* vgen = &bar->gen;
+        unsigned int g = *vgen;
+        __threadfence();
+        unsigned int arrived = atomicAdd(&bar->count, 1u);
+        if (arrived == (unsigned)nact - 1) {
+          bar->count = 0;
+          __threadfence();
+          atomicAdd(&bar->gen, 1u);
+        } else {
+          long long polls = 0;
+          while (*vgen == g) {
+            if (++polls > (1ll << 26) || *(volatile int*)&bar->err) {
+              atomicExch(&bar->err, 1);
+              break;
+            }
+            __nanosleep(20);
+          }
+        }
+        __threadfence();
+        s_ok = (*(volatile int*)&bar->err) == 0;
+      }
+      __syncthreads();
+      if (!s_ok) return;
+    }
+    // 4. w = x + alpha2 v becomes the pending update (relative to rows >= k+1)
     double2 xv = make_double2(0.0, 0.0);
-    for (int q = 0; q < nb; ++q) {
-      xv.x += ((double2*)partial)[q].x;
-      xv.y += ((double2*)partial)[q].y;
+    for (int q = 0; q < nact; ++q) {
+      xv.x += pb[q].x;
+      xv.y += pb[q].y;
     }
-    // alpha2 = -tau/2 * (x^H v); w = x + alpha2 v
     T xvT;
     if constexpr (sizeof(T) == 8) {
       double t1 = xv.x;
@@ -232,27 +300,37 @@ __global__ void __launch_bounds__(kTriThreads)
     } else {
       xvT = *(T*)&xv;
     }
-    T alpha2 = cscale(cmulv(tk, xvT), -0.5);
-    // rank-2 update of A22 (both triangles): A[i, j] -= v_i conj(w_j) + w_i conj(v_j)
-    const size_t mm = (size_t)m * m;
-    for (size_t t = gtid; t < mm; t += gnt) {
-      int i = int(t % m), j = int(t / m);
-      T wi = cadd(xbuf[i], cmulv(alpha2, v[i]));
-      T wj = cadd(xbuf[j], cmulv(alpha2, v[j]));
-      T* p = A + (size_t)(k + 1 + j) * n + (k + 1 + i);
-      *p = csub(*p, cadd(cmulv(v[i], cconj(wj)), cmulv(wi, cconj(v[j]))));
+    const T alpha2 = cscale(cmulv(tk, xvT), -0.5);
+    // reflector storage below the subdiagonal of column k: every CTA has read column k
+    // before the barrier, and it is not read again
+    if (b == 0)
+      for (int r = tid + 1; r < m; r += nt) A[(size_t)k * n + (k + 1 + r)] = vcur[r];
+    __syncthreads();
+    for (int r = tid; r < m; r += nt) {
+      vprev[r] = vcur[r];
+      wprev[r] = active ? cadd(xb[r], cmulv(alpha2, vcur[r])) : czero<T>();
     }
-    // store the reflector below the subdiagonal (column k is no longer read)
-    if (b == nb - 1)
-      for (int i = tid + 1; i < m; i += nt) col[k + 1 + i] = v[i];
-    if (!grid_sync(bar)) return;
+    has_prev = active;
+    __syncthreads();
   }
   if (b == 0 && tid == 0) {
+    // last 2 x 2 block with the pending update of step n-3 (relative to rows >= n-2)
+    auto upd = [&](int i, int j) -> T {
+      T a = A[i + (size_t)j * n];
+      if (has_prev && n >= 3)
+        a = csub(a, cadd(cmulv(vprev[i - (n - 2)], cconj(wprev[j - (n - 2)])),
+                         cmulv(wprev[i - (n - 2)], cconj(vprev[j - (n - 2)]))));
+      return a;
+    };
     if (n >= 2) {
-      d[n - 2] = cre(A[(n - 2) + (size_t)(n - 2) * n]);
-      e[n - 2] = cre(A[(n - 1) + (size_t)(n - 2) * n]);
+      T a11 = upd(n - 2, n - 2), a21 = upd(n - 1, n - 2), a22 = upd(n - 1, n - 1);
+      d[n - 2] = cre(a11);
+      e[n - 2] = cre(a21);
+      d[n - 1] = cre(a22);
+      A[(n - 1) + (size_t)(n - 2) * n] = a21;
+    } else {
+      d[0] = cre(A[0]);
     }
-    d[n - 1] = cre(A[(n - 1) + (size_t)(n - 1) * n]);
   }
 }
 
@@ -447,27 +525,35 @@ __global__ void merge_rot_kernel(double* Q, int n, const MergeDesc* md, int mi, 
   }
 }
 
-// Secular roots: thread j of the grid handles root j of the merge.  Dk, zk: the
-// non-deflated poles (ascending) and weights; Delta[i * k + j] = Dk[j] - lambda_i.
+// Secular roots: one warp per root.  Root i of 1 + rho sum_j z_j^2 / (D_j - lambda) lies
+// in (D_i, D_{i+1}) (the last one in (D_{k-1}, D_{k-1} + rho)); it is represented as
+// origin + tau with the origin at the nearer pole, so D_j - lambda = (D_j - origin) - tau
+// is exact enough for the Gu-Eisenstat vectors.  Iteration: the two-pole rational model
+// of Bunch, Nielsen and Sorensen (psi for poles j <= i, phi for j > i, each matched in
+// value and slope at tau), solved as a quadratic inside the bracket; bisection when the
+// model step leaves the bracket.  Delta[i * k + j] = D_j - lambda_i.
 __global__ void secular_kernel(const double* Dk, const double* zk, int k, double rho, double* lam,
                                double* Delta) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= k) return;
   const double eps = 2.220446049250313e-16;
   int org;
   double lo, hi;
   if (i < k - 1) {
     double gap = Dk[i + 1] - Dk[i];
-    double mid = Dk[i] + 0.5 * gap;
-    double f = 1.0;
-    for (int j = 0; j < k; ++j) f += rho * zk[j] * zk[j] / (Dk[j] - mid);
+    double mid = 0.5 * gap;  // relative to D_i
+    double f = 0.0;
+    for (int j = lane; j < k; j += 32) f += rho * zk[j] * zk[j] / ((Dk[j] - Dk[i]) - mid);
+    for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+    f += 1.0;
     if (f >= 0) {
       org = i;
       lo = 0.0;
-      hi = 0.5 * gap;
+      hi = mid;
     } else {
       org = i + 1;
-      lo = -0.5 * gap;
+      lo = -mid;
       hi = 0.0;
     }
   } else {
@@ -476,53 +562,105 @@ __global__ void secular_kernel(const double* Dk, const double* zk, int k, double
     hi = rho;
   }
   const double dorg = Dk[org];
+  const double ddi = Dk[i] - dorg;
+  const double ddi1 = (i < k - 1) ? Dk[i + 1] - dorg : 0.0;
   double tau = 0.5 * (lo + hi);
-  for (int it = 0; it < 200; ++it) {
-    double f = 1.0, fp = 0.0, fa = 1.0;
-    for (int j = 0; j < k; ++j) {
+  for (int it = 0; it < 100; ++it) {
+    double psi = 0.0, dpsi = 0.0, phi = 0.0, dphi = 0.0, fa = 0.0;
+    for (int j = lane; j < k; j += 32) {
       double del = (Dk[j] - dorg) - tau;
       double q = zk[j] / del;
       double term = rho * zk[j] * q;
-      f += term;
+      double dterm = rho * q * q;
+      if (j <= i) {
+        psi += term;
+        dpsi += dterm;
+      } else {
+        phi += term;
+        dphi += dterm;
+      }
       fa += fabs(term);
-      fp += rho * q * q;
     }
+    for (int o = 16; o > 0; o >>= 1) {
+      psi += __shfl_xor_sync(0xffffffffu, psi, o);
+      dpsi += __shfl_xor_sync(0xffffffffu, dpsi, o);
+      phi += __shfl_xor_sync(0xffffffffu, phi, o);
+      dphi += __shfl_xor_sync(0xffffffffu, dphi, o);
+      fa += __shfl_xor_sync(0xffffffffu, fa, o);
+    }
+    double f = 1.0 + psi + phi;
     if (f > 0)
       hi = tau;
     else
       lo = tau;
-    if (fabs(f) <= 4.0 * eps * k * fa) break;
-    double tn = tau - f / fp;
+    if (fabs(f) <= 4.0 * eps * (k + 1.0) * (1.0 + fa)) break;
+    if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi)) || hi - lo < 1e-300) break;
+    // rational model step
+    double tn;
+    double di = ddi - tau;  // distance to the left pole (< 0 ... > 0 by side)
+    double b1 = dpsi * di * di, a1 = psi - b1 / di;
+    if (i < k - 1) {
+      double di1 = ddi1 - tau;
+      double b2 = dphi * di1 * di1, a2 = phi - b2 / di1;
+      double C = 1.0 + a1 + a2;
+      // C (ddi - x)(ddi1 - x) + b1 (ddi1 - x) + b2 (ddi - x) = 0
+      double qa = C, qb = -(C * (ddi + ddi1) + b1 + b2), qc = C * ddi * ddi1 + b1 * ddi1 + b2 * ddi;
+      tn = NAN;
+      if (qa != 0.0) {
+        double disc = qb * qb - 4.0 * qa * qc;
+        if (disc >= 0.0) {
+          double sq = sqrt(disc);
+          double qq = -0.5 * (qb + copysign(sq, qb));
+          double r1 = qq / qa, r2 = (qq != 0.0) ? qc / qq : NAN;
+          if (r1 > lo && r1 < hi)
+            tn = r1;
+          else if (r2 > lo && r2 < hi)
+            tn = r2;
+        }
+      } else if (qb != 0.0) {
+        tn = -qc / qb;
+      }
+    } else {
+      // 1 + phi_const + a1 + b1/(ddi - x) = 0 with phi == 0
+      double C = 1.0 + a1 + phi;
+      tn = (C != 0.0) ? ddi + b1 / C : NAN;
+    }
     if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
-    if (tn == tau || hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi))) break;
+    if (tn == tau) break;
     tau = tn;
   }
-  lam[i] = dorg + tau;
-  for (int j = 0; j < k; ++j) Delta[(size_t)i * k + j] = (Dk[j] - dorg) - tau;
+  if (lane == 0) lam[i] = dorg + tau;
+  for (int j = lane; j < k; j += 32) Delta[(size_t)i * k + j] = (Dk[j] - dorg) - tau;
 }
 
-// Gu-Eisenstat: zhat_j^2 = (lam_j - D_j)/rho * prod_{i != j} (lam_i - D_j)/(D_i - D_j)
+// Gu-Eisenstat: zhat_j^2 = (lam_j - D_j)/rho * prod_{i != j} (lam_i - D_j)/(D_i - D_j);
+// one warp per j, the product accumulated in logarithm-free pairs per lane.
 __global__ void gu_eisenstat_kernel(const double* Dk, const double* zk, int k, double rho, const double* Delta,
                                     double* zh) {
-  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (j >= k) return;
-  double p = -Delta[(size_t)j * k + j] / rho;
-  for (int i = 0; i < k; ++i)
+  double p = 1.0;
+  for (int i = lane; i < k; i += 32)
     if (i != j) p *= (-Delta[(size_t)i * k + j]) / (Dk[i] - Dk[j]);
-  zh[j] = copysign(sqrt(fmax(p, 0.0)), zk[j]);
+  for (int o = 16; o > 0; o >>= 1) p *= __shfl_xor_sync(0xffffffffu, p, o);
+  p *= -Delta[(size_t)j * k + j] / rho;
+  if (lane == 0) zh[j] = copysign(sqrt(fmax(p, 0.0)), zk[j]);
 }
 
-// S^T (k x k, column-major: column i = normalised eigenvector of root i)
+// S^T (k x k, column-major: column i = normalised eigenvector of root i); warp per i
 __global__ void secular_vectors_kernel(const double* zh, int k, const double* Delta, double* St) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (i >= k) return;
   double nrm = 0.0;
-  for (int j = 0; j < k; ++j) {
+  for (int j = lane; j < k; j += 32) {
     double s = zh[j] / Delta[(size_t)i * k + j];
     nrm += s * s;
   }
+  for (int o = 16; o > 0; o >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
   nrm = 1.0 / sqrt(nrm);
-  for (int j = 0; j < k; ++j) St[j + (size_t)i * k] = zh[j] / Delta[(size_t)i * k + j] * nrm;
+  for (int j = lane; j < k; j += 32) St[j + (size_t)i * k] = zh[j] / Delta[(size_t)i * k + j] * nrm;
 }
 
 // Gather the non-deflated (rotated) columns of the block into a contiguous nb x k matrix
@@ -639,20 +777,25 @@ __global__ void scale_rows_phase_kernel(double2* Z, int64_t rows, int64_t cols, 
   }
 }
 
-// compact WY: T factor (upper triangular, nbk x nbk) for reflectors k0..k0+nbk-1 from
-// S = V^H V (nbk x nbk): T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] S[0:j, j]
+// compact WY: T factor (upper triangular, nbk x nbk <= 32) for reflectors k0..k0+nbk-1
+// from S = V^H V: T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] S[0:j, j]; lane i owns row i.
 template <typename T>
 __global__ void wy_tfactor_kernel(const T* S, int nbk, const T* tau, T* Tm) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int i = threadIdx.x;
+  if (blockIdx.x != 0 || i >= 32) return;
+  for (int j = 0; j < nbk; ++j) {
+    if (i < nbk) Tm[i + j * nbk] = czero<T>();
+  }
+  __syncwarp();
   for (int j = 0; j < nbk; ++j) {
     T tj = tau[j];
-    for (int i = 0; i < nbk; ++i) Tm[i + j * nbk] = czero<T>();
-    Tm[j + j * nbk] = tj;
-    for (int i = 0; i < j; ++i) {
-      T acc = czero<T>();
+    T acc = czero<T>();
+    if (i < j)
       for (int l = i; l < j; ++l) acc = cadd(acc, cmulv(Tm[i + l * nbk], S[l + j * nbk]));
-      Tm[i + j * nbk] = cscale(cmulv(tj, acc), -1.0);
-    }
+    __syncwarp();
+    if (i < j) Tm[i + j * nbk] = cscale(cmulv(tj, acc), -1.0);
+    if (i == j) Tm[j + j * nbk] = tj;
+    __syncwarp();
   }
 }
 
@@ -787,7 +930,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       if (k > 0) {
         DevBuf Delta(c, sizeof(double) * (size_t)k * k), zh(c, sizeof(double) * k),
             St(c, sizeof(double) * (size_t)k * k);
-        int tb = 64, gb = (k + tb - 1) / tb;
+        int tb = 256, gb = (k * 32 + tb - 1) / tb;  // one warp per root
         secular_kernel<<<gb, tb, 0, c->stream>>>(Dk.as<double>(), zk.as<double>(), k, rho[mi], lam.as<double>(),
                                                  Delta.as<double>());
         gu_eisenstat_kernel<<<gb, tb, 0, c->stream>>>(Dk.as<double>(), zk.as<double>(), k, rho[mi],
@@ -925,15 +1068,15 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
   } else {
     // cooperative tridiagonalisation
     int max_blocks = 0;
-    size_t shm = eb * n;
-    if (shm > 48 * 1024)
-      NSG_CUDA(cudaFuncSetAttribute(tridiag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    size_t shm = eb * 3 * n;
+    NSG_CHECK(shm <= 200 * 1024, NSG_ERR_UNSUPPORTED, "tridiagonalisation: matrix order too large");
+    NSG_CUDA(cudaFuncSetAttribute(tridiag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
     NSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks, tridiag_kernel<T>, kTriThreads, shm));
     NSG_CHECK(max_blocks > 0, NSG_ERR_UNSUPPORTED, "tridiagonalisation: no resident block fits");
     int64_t want = ((int64_t)n * n + kTriThreads * 8 - 1) / (kTriThreads * 8);
     int grid = int(std::min<int64_t>({(int64_t)max_blocks * c->num_sms, std::max<int64_t>(want, 1),
-                                      (int64_t)c->num_sms * 2}));
-    DevBuf xbuf(c, eb * n), part(c, sizeof(double2) * grid), bar(c, sizeof(Barrier));
+                                      (int64_t)c->num_sms}));
+    DevBuf xbuf(c, eb * 2 * n), part(c, sizeof(double2) * 2 * grid), bar(c, sizeof(Barrier));
     NSG_CUDA(cudaMemsetAsync(bar.p, 0, sizeof(Barrier), c->stream));
     double* pd = dd.as<double>();
     double* pe = de.as<double>();

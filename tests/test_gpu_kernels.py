@@ -109,7 +109,8 @@ def test_factorize_truncation(nsg_ctx, cplx, m, n):
         s = np.linalg.svd(M, compute_uv=False)
         kref, errref = ol.truncate_spectrum(s ** 2, cutoff, maxdim)
         assert info["newdim"] == kref
-        assert abs(info["truncerr"] - errref) <= 1e-9 * max(errref, 1e-16) + 1e-15
+        # the Gram route fixes each discarded sigma^2 to ~1e-15 of ||M||^2 (absolute)
+        assert abs(info["truncerr"] - errref) <= 1e-6 * errref + 1e-14
         u = U.to_numpy()
         c = Cc.to_numpy()
         assert np.allclose(u.conj().T @ u, np.eye(kref), atol=1e-12)
