@@ -1,0 +1,310 @@
+"""Benchmark: 2-site DMRG sweeps on the N=100 Heisenberg chain on one GB300.
+
+Workload (the "large 2-site DMRG" configuration): S=1/2 Heisenberg chain N=100, J=1,
+open boundaries, MPO bond dimension 5; random MPS at bond dimension 32 from seed 1
+(own PCG64 generator); maxdim schedule [64, 128, 256, 512, 1024] by sweep, cutoff
+1e-12, densitymatrix subspace expansion on, Lanczos krylovdim 3 / maxiter 1.
+One step = one full sweep (198 two-site regions).  Warm-up steps are the first W sweeps
+of the schedule, the timed steps the next K sweeps.  Metric: sweeps/s (higher is
+better); the split-precision form (TF32x3 contractions on tcgen05, FP64 Gram matrix,
+eigensolver and Lanczos scalars) is the product path, `--precision fp64` the plain form.
+
+Timing: CUDA events on the library's stream around each timed sweep; the per-kernel
+roofline comes from events around each launch of the dominant kernel classes in the
+same region.  Inputs larger than L2: the two-site tensors, environments and GEMM
+operands at bond dimension >= 512 are 8-170 MB each and are rewritten every region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_SITES, CHI0, SEED = 100, 32, 1
+SCHEDULE = [64, 128, 256, 512, 1024]
+CUTOFF = 1e-12
+REGIONS_PER_SWEEP = 2 * (N_SITES - 1)
+
+
+def peaks():
+    f = ROOT / "MEASURED_PEAKS.json"
+    if f.exists():
+        d = json.loads(f.read_text())
+        return d.get("bf16_tflops"), d.get("hbm_gbs"), "measured"
+    return 1900.0, 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self):
+        self.rows, self.proc = [], None
+
+    def start(self):
+        cmd = ["nvidia-smi", "--query-gpu=index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+               "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+               "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+               "--format=csv,noheader,nounits", "-lms", "200"]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = [r for r in self.rows if len(r) >= 9]
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace('.', '', 1).isdigit())
+        mx = max(float(r[2]) for r in rows if r[2].replace('.', '', 1).isdigit())
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k].strip() == "Active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": reasons,
+                "samples": len(rows)}
+
+
+def workload():
+    import networksolvers_gb300.models as m
+    return m.heisenberg_chain(N_SITES), m.random_state(m.chain_graph(N_SITES), CHI0, seed=SEED)
+
+
+def kwargs_for(sweep_offset=0):
+    sched = SCHEDULE[sweep_offset:] if sweep_offset < len(SCHEDULE) else [SCHEDULE[-1]]
+    trunc = dict(cutoff=CUTOFF, maxdim=sched)
+    return dict(nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+                extracter_kwargs=dict(trunc=trunc, subspace_algorithm="densitymatrix"),
+                inserter_kwargs=dict(trunc=trunc))
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle on a bounded steady-state sample (one region step at
+# bond dimension 1024: 3 H_eff applications in Lanczos, truncated SVD, environment update)
+# ---------------------------------------------------------------------------
+
+
+def cpu_region_sample(nregions=2, chi=1024, seed=7):
+    from oracle import krylov as ok, linalg as ol
+    from oracle.tensor import Index, Tensor
+    import networksolvers_gb300.models as m
+    rng = np.random.default_rng(seed)
+    W = m.heisenberg_chain(4).tensors[2]  # bulk MPO tensor [left, s', s, right], w = 5
+    w, d = W.shape[0], W.shape[1]
+    a, b, s1, s2 = Index(chi), Index(chi), Index(d), Index(d)
+    w1, w2, w3 = Index(w), Index(w), Index(w)
+    L = rng.standard_normal((chi, w, chi)); L = L + L.transpose(2, 1, 0)
+    R = rng.standard_normal((chi, w, chi)); R = R + R.transpose(2, 1, 0)
+    Lt, Rt = Tensor(L, [a.prime(), w1, a]), Tensor(R, [b.prime(), w3, b])
+    W1, W2 = Tensor(W, [w1, s1.prime(), s1, w2]), Tensor(W, [w2, s2.prime(), s2, w3])
+    from oracle.tensor import contract
+    inds = [a, s1, s2, b]
+    hmap = lambda x: contract([Lt, W1, W2, Rt, Tensor(x, inds)], out=[i.prime() for i in inds]).data
+    times = []
+    for _ in range(nregions):
+        x0 = rng.standard_normal((chi, d, d, chi))
+        t = time.perf_counter()
+        lam, x = ok.eigsolve_lanczos(hmap, x0, krylovdim=3, maxiter=1)
+        U, Cc, err, sp = ol.factorize(Tensor(x, inds), [a, s1], cutoff=CUTOFF, maxdim=chi)
+        A = U
+        Lnew = contract([Lt, A, W1, A.dag().prime()], out=[U.inds[-1].prime(), w2, U.inds[-1]])
+        times.append(time.perf_counter() - t)
+    return float(np.mean(times)), nregions
+
+
+def run_reference(args):
+    """CPU reference arm: the oracle (FP64 numpy/OpenBLAS, all host threads)."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    steps = []
+    for k in range(args.warmup + args.steps):
+        t_region, _ = cpu_region_sample(nregions=1, seed=100 + k)
+        if k >= args.warmup:
+            steps.append(t_region * REGIONS_PER_SWEEP)
+    t = float(np.mean(steps))
+    v = 1.0 / t
+    cores = os.cpu_count()
+    line = {"impl": "reference", "metric": "dmrg_sweeps_per_s", "value": v, "unit": "sweeps/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "global_batch": 1,
+                       "seq_len": N_SITES, "parallelism": "none"},
+            "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
+                             "sample": "one steady-state region step per step (bond dim 1024: Lanczos with 3 H_eff "
+                                       "applications, truncated SVD, environment update) x 198 regions per sweep"},
+            "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_nsg(args):
+    import networksolvers_gb300 as ns
+    from networksolvers_gb300 import _native
+    from networksolvers_gb300.sweep import _prepare
+    rank, world = int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = world > 1
+    if dist:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(local)
+        td.init_process_group("nccl")
+    ctx = _native.Context(local, precision=args.precision)
+    _native.set_default_context(ctx)
+    H, psi0 = workload()
+    psi, P = _prepare(H, psi0, ctx)
+    kw = kwargs_for(0)
+    from networksolvers_gb300.sweep import EigsolveProblem, sweep_solve, updater_eigsolve
+    from networksolvers_gb300.network import euler_sweep
+    prob = EigsolveProblem(psi, P)
+    energies, maxdims, sweep_ms = [], [], []
+    plan = lambda: euler_sweep(psi.g, 2, **dict(extracter_kwargs=kw["extracter_kwargs"],
+                                                 updater_kwargs=kw["updater_kwargs"],
+                                                 inserter_kwargs=kw["inserter_kwargs"], outputlevel=0))
+    total = args.warmup + args.steps
+    clocks = Clocks()
+    prof = None
+    launches0 = None
+    for sweep in range(1, total + 1):
+        timed = sweep > args.warmup
+        if timed and sweep == args.warmup + 1:
+            if dist:
+                td.barrier()
+            ctx.synchronize()
+            clocks.start()
+            ctx.profile(True)
+            launches0 = ctx.counters()["launches"]
+        ctx.record(0)
+        # one sweep of the schedule (sweep index drives get_or_last)
+        from networksolvers_gb300.sweep import RegionIterator, region_iterator_action
+        pl = plan()
+        R = RegionIterator(prob, pl)
+        for k, (region, rkws) in enumerate(pl):
+            R.which = k
+            kws = dict(rkws)
+            prob = region_iterator_action(prob, R, updater_eigsolve, sweep=sweep, **kws)
+        ctx.record(1)
+        ms = ctx.elapsed_ms(0, 1)
+        energies.append(prob.eigenvalue)
+        maxdims.append(prob.state.maxlinkdim())
+        if timed:
+            sweep_ms.append(ms)
+    ctx.synchronize()
+    if dist:
+        td.barrier()
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    launches = ctx.counters()["launches"] - launches0
+    clk = clocks.stop()
+    t_sweep = float(np.sum(sweep_ms)) / 1e3
+    if dist:
+        import torch
+        tt = torch.tensor([t_sweep], device="cuda")
+        td.all_reduce(tt, op=td.ReduceOp.MAX)
+        t_sweep = float(tt.item())
+    value = world * args.steps / t_sweep
+    # e2e: one sweep through the public API from host buffers (upload, sweep, download)
+    e2e = None
+    if rank == 0 and not args.no_e2e:
+        arrays = prob.state.to_numpy(psi0)
+        from networksolvers_gb300.models import Network
+        host_state = Network(psi0.graph, arrays, psi0.legs, np.float64, {"kind": "state", "ortho_region": list(psi0.graph.vertices)})
+        h2d = sum(a.nbytes for a in arrays.values()) + sum(t.nbytes for t in H.tensors.values())
+        off = min(args.warmup + args.steps, len(SCHEDULE)) - 1
+        kw2 = kwargs_for(off)
+        t0 = time.perf_counter()
+        E2, psi2 = ns.dmrg(H, host_state, nsweeps=1, **kw2)
+        out = psi2.to_numpy(psi0)
+        t1 = time.perf_counter()
+        d2h = sum(a.nbytes for a in out.values()) + 8
+        e2e = {"value": 1.0 / (t1 - t0), "unit": "sweeps/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+    bf16, hbm, kind = peaks()
+    # roofline of the dominant kernel class in the timed region
+    classes = {k: v for k, v in prof.items() if v["launches"] > 0}
+    dom = max(classes, key=lambda k: classes[k]["ms"]) if classes else None
+    tot_ms = sum(v["ms"] for v in classes.values())
+    roof = None
+    if dom == "tc_gemm":
+        c = classes[dom]
+        achieved = 3.0 * c["flops"] / (c["ms"] / 1e3) / 1e12  # three TF32 products per FP64-equivalent flop
+        peak = bf16 / 2.0
+        roof = {"bound": "tensor", "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                "traffic": None, "kernel": "tc_gemm_tf32x3_kernel",
+                "peak_note": f"bf16 dense ({kind}) / 2 for kind::tf32"}
+    elif dom is not None:
+        c = classes[dom]
+        achieved = c["flops"] / (c["ms"] / 1e3) / 1e12
+        fp64_peak = 1.25
+        roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak, "traffic": None, "kernel": dom,
+                "peak_note": "GB300 FP64 rate (no FP64 figure in the measured peaks; 1.25 TFLOP/s nominal)"}
+    tc = classes.get("tc_gemm")
+    heff_tflops = (tc["flops"] / (tc["ms"] / 1e3) / 1e12) if tc else None
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        t_region, nreg = cpu_region_sample(nregions=1)
+        cpu = {"value": 1.0 / (t_region * REGIONS_PER_SWEEP), "unit": "sweeps/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": f"{nreg} steady-state region step(s) at bond dimension 1024 (Lanczos with "
+                                         f"3 H_eff applications, truncated SVD, environment update) x 198 regions"}
+    if rank == 0:
+        line = {"metric": "dmrg_sweeps_per_s", "value": value, "unit": "sweeps/s", "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sweep * 1e3 / args.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64" if args.precision == "fp64" else f"{args.precision}+f64",
+                "data": "synthetic",
+                "config": {"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "global_batch": world,
+                           "seq_len": N_SITES, "parallelism": f"replicas{world}",
+                           "timed_sweeps": list(range(args.warmup + 1, args.warmup + args.steps + 1)),
+                           "maxdim_schedule": SCHEDULE, "precision": args.precision,
+                           "l2": "operands 8-170 MB per GEMM at bond dim >= 512 (larger than L2)"},
+                "energy": energies[-1], "energies_per_sweep": energies, "maxlinkdim_per_sweep": maxdims,
+                "sweep_ms": sweep_ms, "heff_gemm_tflops_fp64_equiv": heff_tflops,
+                "kernel_share": {k: v["ms"] / tot_ms for k, v in classes.items()} if tot_ms else {},
+                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if dist:
+        td.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=2)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="nsg", choices=["nsg", "reference"])
+    ap.add_argument("--precision", default="tf32x3", choices=["tf32x3", "fp64"])
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        raise SystemExit("warmup must be >= 3")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_nsg(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -79,6 +79,22 @@ int nsg_ctx_memory(const nsg_ctx* ctx, uint64_t* in_use, uint64_t* peak, uint64_
  * [2] = contraction calls, [3] = linear-map applications; reset if `reset`. */
 int nsg_ctx_counters(nsg_ctx* ctx, uint64_t* counters4, int reset);
 
+/* Device-side timing on the context's stream: record event `slot` (0..15); elapsed
+ * milliseconds between two recorded slots (synchronises on the later one). */
+int nsg_ctx_event_record(nsg_ctx* ctx, int slot);
+int nsg_ctx_event_elapsed(nsg_ctx* ctx, int slot_from, int slot_to, float* ms);
+/* Per-kernel-class profiling: while enabled, launches of the classes below are
+ * bracketed by CUDA events on the context's stream.  Reading synchronises and returns
+ * the launch count, the summed device milliseconds and the summed algorithmic flops
+ * (real flops; for tensor-core GEMMs the FP64-equivalent 2*M*N*K). Enabling resets. */
+#define NSG_PROF_TC_GEMM 0     /* tcgen05 split-precision GEMM kernel              */
+#define NSG_PROF_SPLIT 1       /* FP64 -> TF32 slice pass                          */
+#define NSG_PROF_SIMT_GEMM 2   /* FP64 CUDA-core GEMM                              */
+#define NSG_PROF_TRIDIAG 3     /* Householder tridiagonalisation                   */
+#define NSG_PROF_NCLASS 4
+int nsg_ctx_profile(nsg_ctx* ctx, int enable);
+int nsg_ctx_profile_read(nsg_ctx* ctx, int cls, uint64_t* launches, double* ms, double* flops);
+
 /* ---- tensors ------------------------------------------------------------- */
 int nsg_tensor_create(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims, nsg_tensor** out);
 int nsg_tensor_upload(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims,

@@ -42,6 +42,10 @@ _SIGS = {
     "nsg_ctx_synchronize": (i32, [p]),
     "nsg_ctx_memory": (i32, [p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
     "nsg_ctx_counters": (i32, [p, C.POINTER(u64), i32]),
+    "nsg_ctx_event_record": (i32, [p, i32]),
+    "nsg_ctx_event_elapsed": (i32, [p, i32, i32, C.POINTER(C.c_float)]),
+    "nsg_ctx_profile": (i32, [p, i32]),
+    "nsg_ctx_profile_read": (i32, [p, i32, C.POINTER(u64), P_dbl, P_dbl]),
     "nsg_tensor_create": (i32, [p, i32, i32, P_i64, P_p]),
     "nsg_tensor_upload": (i32, [p, i32, i32, P_i64, p, P_p]),
     "nsg_tensor_download": (i32, [p, p, p]),
@@ -128,6 +132,26 @@ class Context:
         arr = (u64 * 4)()
         self.check(self.L.nsg_ctx_counters(self.h, arr, int(reset)))
         return {"launches": arr[0], "flops": arr[1], "contractions": arr[2], "applies": arr[3]}
+
+    def record(self, slot):
+        self.check(self.L.nsg_ctx_event_record(self.h, slot))
+
+    def elapsed_ms(self, a, b):
+        f = C.c_float()
+        self.check(self.L.nsg_ctx_event_elapsed(self.h, a, b, C.byref(f)))
+        return f.value
+
+    def profile(self, enable):
+        self.check(self.L.nsg_ctx_profile(self.h, int(enable)))
+
+    def profile_read(self):
+        names = ["tc_gemm", "split", "simt_gemm", "tridiag"]
+        out = {}
+        for k, nm in enumerate(names):
+            n, ms, fl = u64(), dbl(), dbl()
+            self.check(self.L.nsg_ctx_profile_read(self.h, k, C.byref(n), C.byref(ms), C.byref(fl)))
+            out[nm] = dict(launches=n.value, ms=ms.value, flops=fl.value)
+        return out
 
     def close(self):
         if getattr(self, "h", None):

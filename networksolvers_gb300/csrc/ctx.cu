@@ -116,10 +116,21 @@ int nsg_ctx_create(int device, uint64_t hbm_budget_bytes, nsg_ctx** out) {
   NSG_API_END(c)
 }
 
+static void clear_profile(nsg_ctx* c) {
+  for (auto& r : c->prof) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  c->prof.clear();
+}
+
 int nsg_ctx_destroy(nsg_ctx* c) {
   if (!c) return NSG_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
+  clear_profile(c);
+  for (auto& e : c->events)
+    if (e) cudaEventDestroy(e);
   if (c->host_scalars) cudaFreeHost(c->host_scalars);
   if (c->dev_scratch) cudaFree(c->dev_scratch);
   cudaStreamDestroy(c->stream);
@@ -140,6 +151,52 @@ int nsg_ctx_set_precision(nsg_ctx* c, int precision) {
 int nsg_ctx_synchronize(nsg_ctx* c) {
   NSG_API_BEGIN(c)
   NSG_CUDA(cudaStreamSynchronize(c->stream));
+  NSG_API_END(c)
+}
+
+int nsg_ctx_event_record(nsg_ctx* c, int slot) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && slot >= 0 && slot < 16, NSG_ERR_INVALID, "event slot 0..15");
+  if (!c->events[slot]) NSG_CUDA(cudaEventCreate(&c->events[slot]));
+  NSG_CUDA(cudaEventRecord(c->events[slot], c->stream));
+  NSG_API_END(c)
+}
+
+int nsg_ctx_event_elapsed(nsg_ctx* c, int a, int b, float* ms) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && ms && a >= 0 && a < 16 && b >= 0 && b < 16 && c->events[a] && c->events[b], NSG_ERR_INVALID,
+            "event slots not recorded");
+  NSG_CUDA(cudaEventSynchronize(c->events[b]));
+  NSG_CUDA(cudaEventElapsedTime(ms, c->events[a], c->events[b]));
+  NSG_API_END(c)
+}
+
+int nsg_ctx_profile(nsg_ctx* c, int enable) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c, NSG_ERR_INVALID, "null context");
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  clear_profile(c);
+  c->profiling = enable != 0;
+  NSG_API_END(c)
+}
+
+int nsg_ctx_profile_read(nsg_ctx* c, int cls, uint64_t* launches, double* ms, double* flops) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && cls >= 0 && cls < NSG_PROF_NCLASS, NSG_ERR_INVALID, "profile class out of range");
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  uint64_t n = 0;
+  double t = 0, f = 0;
+  for (auto& r : c->prof) {
+    if (r.cls != cls) continue;
+    float e = 0;
+    NSG_CUDA(cudaEventElapsedTime(&e, r.a, r.b));
+    ++n;
+    t += e;
+    f += r.flops;
+  }
+  if (launches) *launches = n;
+  if (ms) *ms = t;
+  if (flops) *flops = f;
   NSG_API_END(c)
 }
 

@@ -305,6 +305,21 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   const int dt = T->dtype;
   const size_t eb = elem_bytes(dt);
   NSG_CHECK(m <= (1 << 16), NSG_ERR_UNSUPPORTED, "factorize: row space above 65536");
+  // The Gram route squares magnitudes: bring the entries to O(1) first (tensors of
+  // un-normalised networks reach 1e150 and beyond) and scale C back at the end.
+  double mx = amax(c, dt, M->size, M->data);
+  NSG_CHECK(std::isfinite(mx), NSG_ERR_NONFINITE, "factorize: non-finite input");
+  double sc = 1.0;
+  if (mx > 0 && (mx > 1e50 || mx < 1e-50)) {
+    sc = mx;
+    if (!owned) {
+      nsg_tensor* Mc = new_tensor(c, M->dtype, M->rank, M->dims, false);
+      NSG_CUDA(cudaMemcpyAsync(Mc->data, M->data, M->bytes, cudaMemcpyDeviceToDevice, c->stream));
+      M = Mc;
+      owned = true;
+    }
+    scale(c, dt, M->size, 1.0 / sc, 0.0, M->data);
+  }
   // G = M M^H (FP64 in every precision mode: the Gram matrix fixes the truncation)
   void* G = dalloc(c, eb * m * m);
   GemmArgs g;
@@ -371,11 +386,12 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   h.ldc = k;
   h.batch = 1;
   h.strideA = h.strideB = h.strideC = 0;
-  gemm_f64_simt(c, h);
+  h.alpha_re = sc;
+  gemm_f64_simt(c, h);  // FP64: C carries the small singular directions of the next region
   if (owned) free_tensor(c, M);
   if (spectrum)
     for (int64_t i = 0; i < std::min<int64_t>(spectrum_cap, origm); ++i)
-      spectrum[i] = i < int64_t(P.size()) ? std::max(P[i], 0.0) : 0.0;
+      spectrum[i] = i < int64_t(P.size()) ? std::max(P[i], 0.0) * sc * sc : 0.0;
   *U = Ut;
   *C = Ct;
   if (newdim) *newdim = k;

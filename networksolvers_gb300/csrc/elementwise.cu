@@ -219,6 +219,20 @@ __global__ void row_norms_kernel(int64_t rows, int64_t cols, const void* A_, int
   }
 }
 
+__global__ void amax_partial_kernel(int64_t n, const double* __restrict__ x, double* __restrict__ partial) {
+  __shared__ double red[kThreads];
+  double m = 0.0;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x)
+    m = fmax(m, fabs(x[i]));
+  red[threadIdx.x] = m;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + s]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
 template <typename T>
 __global__ void concat_kernel(int64_t pre, int64_t Ka, int64_t Kb, int64_t post, const T* __restrict__ a,
                               const T* __restrict__ b, T* __restrict__ out) {
@@ -356,7 +370,17 @@ double norm2(nsg_ctx* c, int dtype, int64_t n, const void* x) {
   double out[2];
   const void* v[1] = {x};
   multi_dot(c, dtype, n, 1, v, x, out);
-  return std::sqrt(out[0] > 0 ? out[0] : 0.0);
+  if (std::isfinite(out[0]) && out[0] > 1e-280) return std::sqrt(out[0]);
+  // overflow or underflow of the sum of squares: rescale by the largest component
+  double mx = amax(c, dtype, n, x);
+  if (mx == 0.0 || !std::isfinite(mx)) return mx;
+  int64_t nd = dtype == NSG_C128 ? 2 * n : n;
+  double* tmp = (double*)dalloc(c, sizeof(double) * nd);
+  axpby(c, NSG_F64, nd, 1.0 / mx, 0.0, x, 0.0, 0.0, tmp);
+  const void* vt[1] = {tmp};
+  multi_dot(c, NSG_F64, nd, 1, vt, tmp, out);
+  dfree(c, tmp, sizeof(double) * nd);
+  return mx * std::sqrt(out[0] > 0 ? out[0] : 0.0);
 }
 
 void copy_columns(nsg_ctx* c, int dtype, int64_t rows, int64_t ncols, const void* src, int64_t lds,
@@ -379,6 +403,22 @@ void copy_rows(nsg_ctx* c, int dtype, int64_t nrows_out, int64_t ncols, const vo
   size_t eb = elem_bytes(dtype);
   NSG_CUDA(cudaMemcpy2DAsync(dst, ldd * eb, src, lds * eb, nrows_out * eb, ncols, cudaMemcpyDeviceToDevice,
                              c->stream));
+}
+
+double amax(nsg_ctx* c, int dtype, int64_t n, const void* x) {
+  // complex: max over real and imaginary parts (a factor sqrt(2) of the modulus at most)
+  int64_t nd = dtype == NSG_C128 ? 2 * n : n;
+  int nb = grid_for(c, nd, 2);
+  double* scratch = dev_scratch(c, nb);
+  amax_partial_kernel<<<nb, kThreads, 0, c->stream>>>(nd, (const double*)x, scratch);
+  count_launch(c);
+  check_launch("amax");
+  std::vector<double> h(nb);
+  NSG_CUDA(cudaMemcpyAsync(h.data(), scratch, sizeof(double) * nb, cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  double m = 0.0;
+  for (double v : h) m = std::fmax(m, v);
+  return m;
 }
 
 void row_norms2(nsg_ctx* c, int dtype, int64_t rows, int64_t cols, const void* A, int64_t lda, double* out_dev) {

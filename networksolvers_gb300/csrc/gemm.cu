@@ -193,6 +193,8 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   int64_t gz = zt < 65535 ? zt : 65535;
   dim3 grid{unsigned(gx), unsigned(gy), unsigned(gz)};
   const size_t eb = g.dtype == NSG_C128 ? 16 : 8;
+  ProfScope ps(c, NSG_PROF_SIMT_GEMM,
+               double(g.M) * double(g.N) * double(g.K) * double(g.batch) * (g.dtype == NSG_C128 ? 8.0 : 2.0));
   void* W = nullptr;
   size_t wbytes = 0;
   void* Cout = g.C;
@@ -231,7 +233,14 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   check_launch("gemm_f64_simt");
 }
 
-void gemm(nsg_ctx* c, const GemmArgs& g) {
+void gemm(nsg_ctx* c, const GemmArgs& g_in) {
+  GemmArgs g = g_in;
+  if (g.dtype == NSG_F64) {  // conjugation is the identity on real data
+    if (g.opA == OP_C) g.opA = OP_T;
+    if (g.opA == OP_R) g.opA = OP_N;
+    if (g.opB == OP_C) g.opB = OP_T;
+    if (g.opB == OP_R) g.opB = OP_N;
+  }
   double mac = double(g.M) * double(g.N) * double(g.K) * double(g.batch);
   c->flops += uint64_t(mac * (g.dtype == NSG_C128 ? 8.0 : 2.0));
   if (g.K == 0) {

@@ -355,6 +355,7 @@ void split_operand(nsg_ctx* c, const double* src, int64_t rows, int64_t K, int64
                    int64_t batch, int64_t rows_p, int64_t K_p, float* hi, float* lo) {
   int64_t ntiles = ((rows_p + 31) / 32) * (K_p / 32) * batch;
   int grid = int(std::min<int64_t>(ntiles, (int64_t)c->num_sms * 16));
+  ProfScope ps(c, NSG_PROF_SPLIT, 0.0);
   split_tf32_kernel<<<grid, 256, 0, c->stream>>>(src, rows, K, rs, ks, bs, rows_p, K_p, hi, lo, batch);
   count_launch(c);
   check_launch("split_tf32");
@@ -401,7 +402,10 @@ bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g) {
     return false;
   }
   dim3 grid(unsigned(Mp / TM), unsigned(Np / BN), unsigned(g.batch));
+  {
+  ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(g.M) * double(g.N) * double(g.K) * double(g.batch));
   tc_gemm_tf32x3_kernel<<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mAh, mAl, mBh, mBl, int(Kp / BK), ep);
+  }
   count_launch(c);
   check_launch("tc_gemm_tf32x3");
   dfree(c, buf, sizeof(float) * 2 * (szA + szB));

@@ -61,6 +61,14 @@ struct nsg_ctx {
   double* dev_scratch = nullptr;
   size_t dev_scratch_cap = 0;
   int num_sms = 0;
+  cudaEvent_t events[16] = {};
+  bool profiling = false;
+  struct ProfRec {
+    int cls;
+    cudaEvent_t a, b;
+    double flops;
+  };
+  std::vector<ProfRec> prof;
 };
 
 namespace nsg {
@@ -75,6 +83,27 @@ void free_tensor(nsg_ctx* c, nsg_tensor* t);
 double* host_scalars(nsg_ctx* c, size_t n);
 double* dev_scratch(nsg_ctx* c, size_t n);
 inline void count_launch(nsg_ctx* c, int n = 1) { c->launches += n; }
+
+// Brackets a kernel launch with CUDA events while the context is profiling.
+struct ProfScope {
+  nsg_ctx* c;
+  int cls;
+  double flops;
+  cudaEvent_t a = nullptr, b = nullptr;
+  ProfScope(nsg_ctx* cc, int k, double f) : c(cc), cls(k), flops(f) {
+    if (c->profiling) {
+      cudaEventCreate(&a);
+      cudaEventCreate(&b);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~ProfScope() {
+    if (a) {
+      cudaEventRecord(b, c->stream);
+      c->prof.push_back({cls, a, b, flops});
+    }
+  }
+};
 void check_launch(const char* what);
 
 // ---------------------------------------------------------------------------
@@ -107,6 +136,7 @@ void multi_dot(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, c
 void multi_axpy(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v,
                 const double* coef, void* w);
 double norm2(nsg_ctx* c, int dtype, int64_t n, const void* x);
+double amax(nsg_ctx* c, int dtype, int64_t n, const void* x);  // max |component|
 void scale(nsg_ctx* c, int dtype, int64_t n, double ar, double ai, void* x);
 void copy_columns(nsg_ctx* c, int dtype, int64_t rows, int64_t ncols, const void* src,
                   int64_t lds, const int* d_colidx, void* dst, int64_t ldd);

@@ -1085,6 +1085,7 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
     T* pp = part.as<T>();
     Barrier* pb = bar.as<Barrier>();
     void* args[] = {&A, &n, &pd, &pe, &pt, &px, &pp, &pb};
+    ProfScope ps(c, NSG_PROF_TRIDIAG, (sizeof(T) == 16 ? 16.0 : 4.0) / 3.0 * double(n) * n * n);
     NSG_CUDA(cudaLaunchCooperativeKernel((void*)tridiag_kernel<T>, dim3(grid), dim3(kTriThreads), args, shm,
                                          c->stream));
     count_launch(c);

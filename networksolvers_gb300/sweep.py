@@ -169,6 +169,18 @@ def subspace_expand(problem, local, region_iterator, algorithm, trunc, expansion
     if expand <= 0:
         return problem, local
     tr = dict(trunc, maxdim=expand)
+    # the expansion's projections are checked against a 1e-10 orthogonality guard
+    # (densitymatrix.jl:59): its contractions run in FP64 whatever the context's mode
+    ctx = A.ctx
+    prec = ctx.precision
+    ctx.set_precision("fp64")
+    try:
+        return _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass)
+    finally:
+        ctx.set_precision(prec)
+
+
+def _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass):
     parts = [A]
     for (u, v) in P.incident_edges(P.pos):
         if u in region or v in region:

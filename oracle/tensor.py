@@ -149,7 +149,7 @@ def contract(tensors, out=None):
         tuple(lab[i] for i in free),)
     path = _paths.get(sig)
     if path is None:
-        path = np.einsum_path(*args, optimize="optimal")[0][1:]
+        path = np.einsum_path(*args, optimize=("optimal", float(2 ** 62)))[0][1:]
         _paths[sig] = path
     # pairwise contractions in the optimal order, each one a BLAS tensordot
     work = list(tensors)

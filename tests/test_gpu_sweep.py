@@ -100,3 +100,39 @@ def test_tdvp_exact_evolution(nsg_ctx):
     dense = full.permute([psi.siteind(v) for v in g.vertices]).to_numpy().reshape(-1)
     fid = abs(np.vdot(vt, dense)) / np.linalg.norm(dense)
     assert fid > 1 - 1e-8
+
+
+def _record_dmrg(run, H, psi0, **kw):
+    rec = []
+
+    def cb(prob, sweep, region, which, **k):
+        rec.append((sweep, which, prob.eigenvalue, prob.last_insert.get("newdim", -1)))
+
+    E, psi = run(H, psi0, region_callback=cb, **kw)
+    return E, np.array(rec), psi
+
+
+@pytest.mark.parametrize("precision", ["fp64", "tf32x3"])
+def test_c3_style_schedule_with_densitymatrix(nsg_ctx, precision):
+    """The large-DMRG recipe at reduced size: Heisenberg N=30, random MPS chi=8 seed 1,
+    maxdim schedule [8, 16, 32], cutoff 1e-12, densitymatrix expansion, 2-site.
+    FP64: per-region energies 1e-10 and bond dimensions exact vs the oracle.
+    TF32x3 (FP32-accumulated contractions): final energy within 1e-5 relative — the
+    environments carry the accumulated left/right energies, so 24-bit accumulation
+    limits the absolute error of H_eff x to ~5e-7 |E|."""
+    from oracle import sweep as osw
+    H, psi0 = m.heisenberg_chain(30), m.random_state(m.chain_graph(30), 8, seed=1)
+    trunc = dict(cutoff=1e-12, maxdim=[8, 16, 32])
+    kw = dict(nsweeps=4, nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+              extracter_kwargs=dict(trunc=trunc, subspace_algorithm="densitymatrix"),
+              inserter_kwargs=dict(trunc=trunc))
+    Eo, ro, _ = _record_dmrg(osw.dmrg, H, psi0, **kw)
+    nsg_ctx.set_precision(precision)
+    try:
+        E, r, psi = _record_dmrg(ns.dmrg, H, psi0, **kw)
+    finally:
+        nsg_ctx.set_precision("fp64")
+    if precision == "fp64":
+        assert np.array_equal(r[:, 3], ro[:, 3])
+        assert np.max(np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])) < 1e-10
+    assert abs(E - Eo) / abs(Eo) < (1e-10 if precision == "fp64" else 1e-5)
