@@ -54,10 +54,11 @@ extern "C" {
 #define NSG_F64 0                /* real double                             */
 #define NSG_C128 1               /* complex double (re, im interleaved)     */
 
-#define NSG_PREC_FP64 0          /* every contraction in FP64               */
-#define NSG_PREC_TF32X3 1        /* large contractions: 3 TF32 products, FP32 accumulate */
-#define NSG_PREC_BF16X3 2        /* large contractions: 3 BF16 products, FP32 accumulate */
-#define NSG_PREC_BF16X6 3        /* large contractions: 6 BF16 products, FP32 accumulate */
+#define NSG_PREC_FP64 0          /* every contraction in FP64 on the CUDA cores           */
+#define NSG_PREC_TF32X3 1        /* large contractions: 3 TF32 products, FP32 accumulate  */
+#define NSG_PREC_OZAKI 2         /* large contractions: 6 BF16 slices per operand, 21
+                                    products, exact FP32 accumulation per 128-deep chunk:
+                                    FP64-level accuracy on the tensor cores              */
 
 #define NSG_MAX_RANK 16
 

@@ -247,7 +247,8 @@ void gemm(nsg_ctx* c, const GemmArgs& g_in) {
     // C = beta*C (alpha term vanishes)
     return;
   }
-  if (c->precision != NSG_PREC_FP64 && gemm_split_tc(c, g)) return;
+  if (c->precision == NSG_PREC_TF32X3 && gemm_split_tc(c, g)) return;
+  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g)) return;
   gemm_f64_simt(c, g);
 }
 

@@ -1,0 +1,440 @@
+// FP64-accurate GEMM on the BF16 tensor cores by exact multi-slice splitting
+// (the Ozaki scheme: K. Ozaki, T. Ogita, S. Oishi, S. M. Rump, "Error-free
+// transformations of matrix multiplication by using fast routines of matrix
+// multiplication and its applications", Numer. Algorithms 59 (2012)).
+//
+// Row i of A is scaled by sigma_i = 2^ceil(log2 max_k |A_ik|) and written as
+//   A_ik / sigma_i = sum_{s<S} 2^{-7(s+1)} A^(s)_ik + r,  A^(s) integers, |A^(s)| <= 128,
+// (round-to-nearest digits, |r| <= 2^{-7S-1}); columns of B likewise with tau_j.  Then
+//   (AB)_ij = sigma_i tau_j sum_g 2^{-7(g+2)} sum_{s+t=g} (A^(s) B^(t))_ij,   g <= S-1.
+// The integer slices are exact in BF16, and with g+1 <= 6 products per group and K
+// chunks of 128 every partial sum is an integer below 2^24, so the tcgen05 FP32
+// accumulation of a group over a chunk is exact.  Drain warps add the six group sums
+// of each chunk into double-float (hi, lo) FP32 accumulators; the epilogue widens to
+// FP64 and applies sigma_i tau_j, alpha and beta.  With S = 6 slices the result is
+// within ~2^-43 K sigma_i tau_j of A B (dropped slices and products).
+//
+// Kernel layout: 128 x 64 output tile per CTA, 16 drain warps (4 warpgroups, each
+// owning 16 accumulator columns) + 1 TMA/MMA warp; three-stage ring of 32-wide K slabs
+// holding all six slices of A and B (SWIZZLE_64B); 6 x 64 TMEM accumulator columns.
+// All mbarrier waits are bounded; on time-out the CTA raises the error flag, drains its
+// TMA copies (bounded), frees its TMEM and returns.
+#include "nsg_internal.h"
+
+#include <cuda.h>
+#include <cuda_bf16.h>
+
+#include <algorithm>
+#include <mutex>
+
+namespace nsg {
+
+namespace {
+
+constexpr int S = 6;                 // slices per operand
+constexpr int G = S;                 // groups g = s + t in [0, S-1]
+constexpr int BM = 128, BN = 64, BKS = 32;  // K slab: 32 bf16 = 64 bytes
+constexpr int STAGES = 3;
+constexpr int SLICE_A = BM * BKS * 2;       // 8 KB
+constexpr int SLICE_B = BN * BKS * 2;       // 4 KB
+constexpr int STAGE_BYTES = S * (SLICE_A + SLICE_B);  // 72 KB
+constexpr int CHUNK_SLABS = 4;              // K = 128 per exact chunk
+constexpr int NDRAIN_WARPS = 16;
+constexpr int NTHREADS = (NDRAIN_WARPS + 1) * 32;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;
+constexpr long long kWaitLimit = 1ll << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, volatile int* fail) {
+  for (long long i = 0; i < kWaitLimit; ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    if (fail && *fail) return false;
+  }
+  return false;
+}
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar, int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(
+          smem_u32(dst)),
+      "l"((uint64_t)map), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+// K-major operand, 64-byte swizzle: 8-row groups 512 bytes apart
+__device__ __forceinline__ uint64_t sdesc64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;
+  d |= (uint64_t)((512u >> 4) & 0x3FFFu) << 32;
+  d |= (uint64_t)1u << 46;
+  d |= (uint64_t)4u << 61;  // 64-byte swizzle
+  return d;
+}
+__device__ __forceinline__ void mma_bf16(uint32_t tmem_d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          tmem_d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc));
+}
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// scales: scale[b][r] = 2^ceil(log2 max_k |src(r, k)|) (1 for an all-zero row)
+// ---------------------------------------------------------------------------
+__global__ void row_scale_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
+                                 int64_t bs, int64_t rows_p, double* __restrict__ scale, int64_t batch) {
+  // one warp per row; lanes stride over k
+  const int lane = threadIdx.x & 31;
+  const int64_t w = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = (gridDim.x * (int64_t)blockDim.x) >> 5;
+  for (int64_t t = w; t < rows_p * batch; t += nw) {
+    int64_t r = t % rows_p, b = t / rows_p;
+    double m = 0.0;
+    if (r < rows) {
+      const double* base = src + b * bs + r * rs;
+      for (int64_t k = lane; k < K; k += 32) m = fmax(m, fabs(base[k * ks]));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0) {
+      int e = 0;
+      if (m > 0) {
+        frexp(m, &e);  // m = f 2^e, f in [0.5, 1)  ->  m <= 2^e
+      }
+      scale[t] = (m > 0) ? ldexp(1.0, e) : 1.0;
+    }
+  }
+}
+
+// slices: out[(b*S + s)][r][k] (bf16, K-major, padded with zeros)
+__global__ void slice_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
+                             int64_t bs, int64_t rows_p, int64_t K_p, const double* __restrict__ scale,
+                             __nv_bfloat16* __restrict__ out, int64_t batch) {
+  __shared__ double tile[32][33];
+  const int64_t tr = rows_p / 32, tk = K_p / 32;
+  const int64_t ntiles = tr * tk * batch;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int64_t t = blockIdx.x; t < ntiles; t += gridDim.x) {
+    int64_t kt = t % tk, rt = (t / tk) % tr, b = t / (tk * tr);
+    const double* base = src + b * bs;
+    if (ks == 1) {
+      for (int i = ty; i < 32; i += 8) {
+        int64_t r = rt * 32 + i, k = kt * 32 + tx;
+        tile[i][tx] = (r < rows && k < K) ? base[r * rs + k] : 0.0;
+      }
+    } else {
+      for (int j = ty; j < 32; j += 8) {
+        int64_t r = rt * 32 + tx, k = kt * 32 + j;
+        tile[tx][j] = (r < rows && k < K) ? base[r * rs + k * ks] : 0.0;
+      }
+    }
+    __syncthreads();
+    for (int i = ty; i < 32; i += 8) {
+      int64_t r = rt * 32 + i, k = kt * 32 + tx;
+      double x = tile[i][tx] / scale[b * rows_p + r];  // |x| <= 1, exact (power of two)
+      for (int s = 0; s < S; ++s) {
+        double y = x * 128.0;  // next 7 bits to the integer part (exact)
+        double dgt = rint(y);
+        x = y - dgt;           // remainder, |x| <= 1/2, exact
+        size_t o = ((size_t)(b * S + s) * rows_p + r) * K_p + k;
+        out[o] = __float2bfloat16_rn((float)dgt);  // |dgt| <= 128: exact in bf16
+      }
+    }
+    __syncthreads();
+  }
+}
+
+struct OzEpi {
+  double* C;
+  int64_t ldc, sC, M, N;
+  double alpha, beta;
+  const double* sa;  // row scales of A  [batch_a][Mp]
+  const double* sb;  // row scales of B^T [batch_b][Np]
+  int64_t Mp, Np;
+  int a_batched, b_batched;
+  int* err;
+};
+
+__device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
+  float s = hi + x;
+  float bb = s - hi;
+  float e = (hi - (s - bb)) + (x - bb);
+  hi = s;
+  lo += e;
+}
+
+__global__ void __launch_bounds__(NTHREADS, 1)
+    oz_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nk,
+                   OzEpi ep) {
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
+  uint64_t* empty = full + STAGES;
+  uint64_t* accfull = empty + STAGES;
+  uint64_t* accempty = accfull + 1;
+  uint32_t* tmem_slot = (uint32_t*)(accempty + 1);
+  volatile int* fail = (volatile int*)(tmem_slot + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, bz = blockIdx.z;
+  const int nchunks = (nk + CHUNK_SLABS - 1) / CHUNK_SLABS;
+
+  if (tid == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], 1);
+    }
+    mbar_init(accfull, 1);
+    mbar_init(accempty, NDRAIN_WARPS * 32);
+    *fail = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(512));
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == NDRAIN_WARPS) {
+    if (lane == 0) {
+      // kind::f16: D F32 (bits 4-5 = 1), A BF16 (7-9 = 1), B BF16 (10-12 = 1), K-major both
+      const uint32_t idesc =
+          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+      auto a_ptr = [&](int st, int s) { return smem + st * STAGE_BYTES + s * SLICE_A; };
+      auto b_ptr = [&](int st, int s) { return smem + st * STAGE_BYTES + S * SLICE_A + s * SLICE_B; };
+      auto issue = [&](int t, int st) {
+        mbar_expect_tx(&full[st], STAGE_BYTES);
+        const int kc = t * BKS;
+        tma_load_3d(a_ptr(st, 0), &mapA, &full[st], kc, m0, (ep.a_batched ? bz : 0) * S);
+        tma_load_3d(b_ptr(st, 0), &mapB, &full[st], kc, n0, (ep.b_batched ? bz : 0) * S);
+      };
+      const int pre = nk < STAGES ? nk : STAGES;
+      for (int t = 0; t < pre; ++t) issue(t, t);
+      int issued = pre;
+      bool ok = true;
+      for (int c = 0; c < nchunks && ok; ++c) {
+        if (c >= 1 && !mbar_wait(accempty, (c - 1) & 1, fail)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const int t0 = c * CHUNK_SLABS, t1 = min(nk, t0 + CHUNK_SLABS);
+        for (int t = t0; t < t1 && ok; ++t) {
+          const int st = t % STAGES;
+          if (!mbar_wait(&full[st], (t / STAGES) & 1, fail)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+          for (int kk = 0; kk < BKS / 16; ++kk) {
+            const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes inside the 64-byte swizzle atom
+#pragma unroll
+            for (int s = 0; s < S; ++s) {
+              const uint64_t ad = sdesc64(smem_u32(a_ptr(st, s)) + off);
+#pragma unroll
+              for (int u = 0; u + s < G; ++u) {
+                const int g = s + u;
+                // group g's first product of the chunk is (s = 0, u = g) at t = t0, kk = 0
+                mma_bf16(tmem + (uint32_t)(g * BN), ad, sdesc64(smem_u32(b_ptr(st, u)) + off), idesc,
+                         (t == t0 && kk == 0 && s == 0) ? 0u : 1u);
+              }
+            }
+          }
+          mma_commit(&empty[st]);
+          if (t >= 1 && issued < nk) {
+            const int sp = (t - 1) % STAGES;
+            if (!mbar_wait(&empty[sp], ((t - 1) / STAGES) & 1, fail)) {
+              ok = false;
+              break;
+            }
+            issue(issued, sp);
+            ++issued;
+          }
+        }
+        if (!ok) break;
+        mma_commit(accfull);
+      }
+      if (!ok) {
+        *fail = 1;
+        atomicExch(ep.err, 1);
+        for (int t = 0; t < issued; ++t) mbar_wait(&full[t % STAGES], (t / STAGES) & 1, nullptr);
+      }
+    }
+  } else {
+    // drain warps: warpgroup q = warp / 4 owns columns [16 q, 16 q + 16); TMEM lanes 32 (warp % 4) ..
+    const int q = warp >> 2, wl = warp & 3;
+    float hi[16], lo[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) hi[j] = lo[j] = 0.f;
+    const uint32_t lane_base = (uint32_t)(wl * 32) << 16;
+    bool ok = true;
+    for (int c = 0; c < nchunks; ++c) {
+      if (!mbar_wait(accfull, c & 1, fail)) {
+        ok = false;
+        atomicExch(ep.err, 1);
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+#pragma unroll
+      for (int g = 0; g < G; ++g) {
+        uint32_t r[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
+            "%14, %15}, [%16];"
+            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+            : "r"(tmem + lane_base + (uint32_t)(g * BN + 16 * q)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        const float sc = __int_as_float((127 - 7 * (g + 2)) << 23);  // 2^{-7(g+2)}, exact
+#pragma unroll
+        for (int j = 0; j < 16; ++j) two_sum_acc(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+      }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      mbar_arrive(accempty);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {  // renormalise (fast two-sum)
+        float s = hi[j] + lo[j];
+        lo[j] = lo[j] - (s - hi[j]);
+        hi[j] = s;
+      }
+    }
+    if (ok) {
+      const int64_t row = m0 + wl * 32 + lane;
+      if (row < ep.M) {
+        const double sa = ep.sa[(ep.a_batched ? bz : 0) * ep.Mp + row];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int64_t col = n0 + 16 * q + j;
+          if (col < ep.N) {
+            const double sb = ep.sb[(ep.b_batched ? bz : 0) * ep.Np + col];
+            const double v = ((double)hi[j] + (double)lo[j]) * sa * sb;
+            double* cp = ep.C + bz * ep.sC + row + col * ep.ldc;
+            *cp = (ep.beta == 0.0) ? ep.alpha * v : fma(ep.alpha, v, ep.beta * (*cp));
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                              CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeFn encode_fn() {
+  static EncodeFn fn = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeFn)p;
+  });
+  return fn;
+}
+
+// slices [planes = batch*S][rows_p][K_p] bf16; box {32, box_rows, S}
+CUtensorMap make_map(void* base, int64_t rows_p, int64_t K_p, int64_t planes, int box_rows) {
+  EncodeFn enc = encode_fn();
+  NSG_CHECK(enc != nullptr, NSG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  CUtensorMap m;
+  cuuint64_t dims[3] = {(cuuint64_t)K_p, (cuuint64_t)rows_p, (cuuint64_t)planes};
+  cuuint64_t strides[2] = {(cuuint64_t)(K_p * 2), (cuuint64_t)(K_p * rows_p * 2)};
+  cuuint32_t box[3] = {(cuuint32_t)BKS, (cuuint32_t)box_rows, (cuuint32_t)S};
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = enc(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, base, dims, strides, box, estr,
+                   CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  NSG_CHECK(r == CUDA_SUCCESS, NSG_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+void slice_operand(nsg_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, int64_t ks, int64_t bs,
+                   int64_t batch, int64_t rows_p, int64_t K_p, double* scale, __nv_bfloat16* out) {
+  {
+    int64_t warps = rows_p * batch;
+    int grid = int(std::min<int64_t>((warps * 32 + 255) / 256, (int64_t)c->num_sms * 16));
+    ProfScope ps(c, NSG_PROF_SPLIT, 0.0);
+    row_scale_kernel<<<grid, 256, 0, c->stream>>>(src, rows, K, rs, ks, bs, rows_p, scale, batch);
+  }
+  int64_t ntiles = (rows_p / 32) * (K_p / 32) * batch;
+  int grid = int(std::min<int64_t>(ntiles, (int64_t)c->num_sms * 16));
+  ProfScope ps(c, NSG_PROF_SPLIT, 0.0);
+  slice_kernel<<<grid, 256, 0, c->stream>>>(src, rows, K, rs, ks, bs, rows_p, K_p, scale, out, batch);
+  count_launch(c, 2);
+  check_launch("ozaki slices");
+}
+
+}  // namespace
+
+bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g) {
+  if (g.dtype != NSG_F64) return false;
+  if (g.opA == OP_C || g.opA == OP_R || g.opB == OP_C || g.opB == OP_R) return false;
+  if (g.M < 64 || g.N < 32 || g.K < 64) return false;
+  if (g.batch > 65535) return false;
+  const int64_t Mp = (g.M + BM - 1) / BM * BM, Np = (g.N + BN - 1) / BN * BN, Kp = (g.K + BKS - 1) / BKS * BKS;
+  const int64_t ars = (g.opA == OP_N) ? 1 : g.lda, aks = (g.opA == OP_N) ? g.lda : 1;
+  const int64_t brs = (g.opB == OP_N) ? g.ldb : 1, bks = (g.opB == OP_N) ? 1 : g.ldb;
+  const int64_t ab = (g.strideA == 0) ? 1 : g.batch, bb = (g.strideB == 0) ? 1 : g.batch;
+  size_t nA = size_t(S) * Mp * Kp * ab, nB = size_t(S) * Np * Kp * bb;
+  size_t bytes = 2 * (nA + nB) + 8 * (size_t(Mp) * ab + size_t(Np) * bb) + 256;
+  unsigned char* buf = (unsigned char*)dalloc(c, bytes);
+  __nv_bfloat16* As = (__nv_bfloat16*)buf;
+  __nv_bfloat16* Bs = As + nA;
+  double* sa = (double*)(((uintptr_t)(Bs + nB) + 255) & ~(uintptr_t)255);
+  double* sb = sa + Mp * ab;
+  slice_operand(c, (const double*)g.A, g.M, g.K, ars, aks, g.strideA, ab, Mp, Kp, sa, As);
+  slice_operand(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
+  CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM), mB = make_map(Bs, Np, Kp, S * bb, BN);
+  int* err = (int*)dev_scratch(c, 1);
+  NSG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  static bool attr = false;
+  if (!attr) {
+    NSG_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr = true;
+  }
+  OzEpi ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, sa, sb, Mp, Np,
+           ab > 1, bb > 1, err};
+  dim3 grid(unsigned(Mp / BM), unsigned(Np / BN), unsigned(g.batch));
+  {
+    ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(g.M) * double(g.N) * double(g.K) * double(g.batch));
+    oz_gemm_kernel<<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, int(Kp / BKS), ep);
+  }
+  count_launch(c);
+  check_launch("oz_gemm");
+  dfree(c, buf, bytes);
+  int herr = 0;
+  NSG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  NSG_CHECK(herr == 0, NSG_ERR_TIMEOUT, "oz_gemm: a bounded mbarrier wait timed out");
+  return true;
+}
+
+}  // namespace nsg

@@ -49,3 +49,29 @@ def test_tf32x3_path_is_the_one_that_ran(nsg_ctx):
         nsg_ctx.set_precision("fp64")
     assert rel(c, a @ b) < 2e-6
     assert after - before == 3
+
+
+@pytest.mark.parametrize("m,k,n", [(128, 64, 64), (200, 100, 300), (1024, 1024, 1024), (130, 4000, 70),
+                                   (5120, 1024, 4096)])
+def test_ozaki_gemm_fp64_level(nsg_ctx, m, k, n):
+    """Six 7-bit BF16 slices per operand, exact FP32 chunk accumulation: FP64-level
+    products (1e-12 relative) in every operand orientation, including rows with a wide
+    dynamic range (one large entry per row, as the environment blocks carry)."""
+    rng = np.random.default_rng(m * 3 + k + n)
+    i, j, l = Index(m), Index(n), Index(k)
+    a = rng.standard_normal((m, k))
+    a[:, 0] *= 1e4
+    b = rng.standard_normal((k, n))
+    ref = a @ b
+    for (ia, aa), (ib, bb) in [(((i, l), a), ((l, j), b)), (((l, i), a.T.copy()), ((l, j), b)),
+                               (((i, l), a), ((j, l), b.T.copy())), (((l, i), a.T.copy()), ((j, l), b.T.copy()))]:
+        A, B = DTensor.from_numpy(aa, ia), DTensor.from_numpy(bb, ib)
+        nsg_ctx.set_precision("ozaki")
+        try:
+            c = contract([A, B], out=[i, j]).to_numpy()
+        finally:
+            nsg_ctx.set_precision("fp64")
+        scale = np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :] * k
+        # the method's bound is relative to the row/column scales (one wide row here)
+        assert np.max(np.abs(c - ref) / scale) < 1e-13, (ia, ib)
+        assert rel(c, ref) < 5e-11
