@@ -171,6 +171,28 @@ int nsg_eigh(nsg_ctx* ctx, const nsg_tensor* rho, const int* row_axes, int n_row
              double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
              double* evals, int64_t evals_cap, int64_t* newdim, double* truncerr);
 
+/* ---- allocation-free GEMM -------------------------------------------------
+ * No counterpart in the reference: an addition for callers that must not allocate
+ * device memory themselves (a Julia program whose CUDA.jl memory pool owns the device,
+ * a host whose caching allocator must account for every byte, a latency-bound caller
+ * that cannot absorb the synchronisation of cudaMalloc/cudaFree).
+ *
+ * C = alpha op(A) op(B) + beta C in the TF32x3 split-precision form of the tensor-core
+ * contractions, for real FP64 column-major matrices already on the current device;
+ * op(X) = X^T when trans* != 0.  Work is ordered on `stream` (NULL = legacy default
+ * stream) and the call synchronises it before returning.  It calls no cudaMalloc,
+ * cudaFree or allocating library routine: the operand slices and the device error
+ * flag live in one static device array of 64 MiB (plus a 256-byte header), held by
+ * every GPU that loads the library until the process exits; sizes whose padded slices
+ * exceed it are rejected with NSG_ERR_UNSUPPORTED.  The first call on a device
+ * resolves that array's address and configures the kernel (with the device current);
+ * make that first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (other streams, other threads) race on it.  On failure the
+ * message is written to errbuf (errlen bytes, NUL-terminated). */
+int nsg_gemm_tf32x3_noalloc(const double* A, int64_t lda, int transA, const double* B, int64_t ldb,
+                            int transB, double* C, int64_t ldc, int64_t M, int64_t N, int64_t K,
+                            double alpha, double beta, void* stream, char* errbuf, int errlen);
+
 #ifdef __cplusplus
 }
 #endif

@@ -21,6 +21,7 @@
 #include <cuda.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 
 namespace nsg {
@@ -417,3 +418,116 @@ bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g) {
 }
 
 }  // namespace nsg
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the TF32x3 split-precision GEMM.
+//
+// Some callers must not allocate device memory behind their own allocator: a Julia
+// program using CUDA.jl hands the device to CUDA.jl's memory pool, which has usually
+// reserved most of HBM already, so a library cudaMalloc can fail or push the pool into
+// out-of-memory; a host that runs this GEMM between operations of its own caching
+// allocator (PyTorch, RMM) wants every byte accounted for by that allocator; and a
+// latency-bound caller cannot afford the device-wide synchronisation cudaMalloc and
+// cudaFree may imply.  For them the slice buffers and the error flag of this GEMM live
+// in one statically sized device array that every GPU loading the library holds until
+// the process exits.
+// ---------------------------------------------------------------------------
+
+namespace nsg {
+namespace {
+
+// 64 MiB of TF32 slices (hi and lo of op(A) and op(B), padded) plus a 256-byte header
+// that holds the device-side error flag.
+constexpr size_t kNoAllocSliceBytes = size_t(64) << 20;
+constexpr size_t kNoAllocHeader = 256;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocHeader + kNoAllocSliceBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+int g_noalloc_sms[kMaxDevices] = {};
+
+void noalloc_error(char* buf, int len, const std::string& msg) {
+  if (buf && len > 0) {
+    size_t n = std::min<size_t>(size_t(len - 1), msg.size());
+    std::memcpy(buf, msg.data(), n);
+    buf[n] = 0;
+  }
+}
+
+}  // namespace
+
+}  // namespace nsg
+
+using namespace nsg;
+
+extern "C" int nsg_gemm_tf32x3_noalloc(const double* A, int64_t lda, int transA, const double* B, int64_t ldb,
+                                       int transB, double* C, int64_t ldc, int64_t M, int64_t N, int64_t K,
+                                       double alpha, double beta, void* stream, char* errbuf, int errlen) {
+  try {
+    NSG_CHECK(A && B && C && M > 0 && N > 0 && K > 0, NSG_ERR_INVALID, "noalloc gemm: null operand or empty size");
+    NSG_CHECK(lda >= (transA ? K : M) && ldb >= (transB ? N : K) && ldc >= M, NSG_ERR_INVALID,
+              "noalloc gemm: leading dimension too small");
+    const int64_t Mp = (M + TM - 1) / TM * TM, Np = (N + BN - 1) / BN * BN, Kp = (K + BK - 1) / BK * BK;
+    const size_t need = sizeof(float) * 2 * size_t(Mp + Np) * size_t(Kp);
+    NSG_CHECK(need <= kNoAllocSliceBytes, NSG_ERR_UNSUPPORTED,
+              "noalloc gemm: operands need " + std::to_string(need) + " bytes of slice scratch, above the static " +
+                  std::to_string(kNoAllocSliceBytes) + "-byte maximum (use the allocating entry points)");
+    int dev = 0;
+    NSG_CUDA(cudaGetDevice(&dev));
+    NSG_CHECK(dev >= 0 && dev < kMaxDevices, NSG_ERR_UNSUPPORTED, "noalloc gemm: device index too large");
+    unsigned char* base = nullptr;
+    int sms = 0;
+    {
+      // one-time set-up per device, with that device current: resolve the static array's
+      // device address and opt the kernel into its shared-memory size
+      std::lock_guard<std::mutex> lk(g_noalloc_mu);
+      if (!g_noalloc_ptr[dev]) {
+        void* p = nullptr;
+        NSG_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        NSG_CUDA(cudaFuncSetAttribute(tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      SMEM_BYTES));
+        NSG_CUDA(cudaDeviceGetAttribute(&g_noalloc_sms[dev], cudaDevAttrMultiProcessorCount, dev));
+        g_noalloc_ptr[dev] = (unsigned char*)p;
+      }
+      base = g_noalloc_ptr[dev];
+      sms = g_noalloc_sms[dev];
+    }
+    cudaStream_t st = (cudaStream_t)stream;
+    int* err = (int*)base;
+    float* Ah = (float*)(base + kNoAllocHeader);
+    float* Al = Ah + size_t(Mp) * Kp;
+    float* Bh = Al + size_t(Mp) * Kp;
+    float* Bl = Bh + size_t(Np) * Kp;
+    // the flag keeps the previous call's value: clear it before this call's kernels
+    NSG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), st));
+    const int64_t ars = transA ? lda : 1, aks = transA ? 1 : lda;
+    const int64_t brs = transB ? 1 : ldb, bks = transB ? ldb : 1;
+    auto split = [&](const double* src, int64_t rows, int64_t rs, int64_t ks, int64_t rows_p, float* hi, float* lo) {
+      int64_t ntiles = ((rows_p + 31) / 32) * (Kp / 32);
+      int grid = int(std::min<int64_t>(ntiles, (int64_t)sms * 16));
+      split_tf32_kernel<<<grid, 256, 0, st>>>(src, rows, K, rs, ks, 0, rows_p, Kp, hi, lo, 1);
+      check_launch("noalloc split_tf32");
+    };
+    split(A, M, ars, aks, Mp, Ah, Al);
+    split(B, N, brs, bks, Np, Bh, Bl);
+    CUtensorMap mAh = make_map(Ah, Mp, Kp, 1, TM), mAl = make_map(Al, Mp, Kp, 1, TM);
+    CUtensorMap mBh = make_map(Bh, Np, Kp, 1, BN), mBl = make_map(Bl, Np, Kp, 1, BN);
+    EpiParams ep{C, ldc, 0, M, N, alpha, beta, err};
+    dim3 grid(unsigned(Mp / TM), unsigned(Np / BN), 1u);
+    tc_gemm_tf32x3_kernel<<<grid, NTHREADS, SMEM_BYTES, st>>>(mAh, mAl, mBh, mBl, int(Kp / BK), ep);
+    check_launch("noalloc tc_gemm_tf32x3");
+    int herr = 0;
+    NSG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+    NSG_CUDA(cudaStreamSynchronize(st));
+    NSG_CHECK(herr == 0, NSG_ERR_TIMEOUT, "noalloc gemm: a bounded mbarrier wait timed out");
+  } catch (const Error& e) {
+    noalloc_error(errbuf, errlen, e.what());
+    return e.code;
+  } catch (const std::exception& e) {
+    noalloc_error(errbuf, errlen, e.what());
+    return NSG_ERR_INVALID;
+  }
+  noalloc_error(errbuf, errlen, "");
+  return NSG_OK;
+}
