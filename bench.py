@@ -289,6 +289,7 @@ def run_nsg(args):
                 "sweep_ms": sweep_ms, "heff_gemm_tflops_fp64_equiv": heff_tflops,
                 "kernel_share": {k: v["ms"] / tot_ms for k, v in classes.items()} if tot_ms else {},
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
+                "launches_before_timed": int(launches0),
                 "clocks": clk}
         print(json.dumps(line), flush=True)
     if dist:

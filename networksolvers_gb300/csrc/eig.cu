@@ -387,7 +387,7 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   h.batch = 1;
   h.strideA = h.strideB = h.strideC = 0;
   h.alpha_re = sc;
-  gemm_f64_simt(c, h);  // FP64: C carries the small singular directions of the next region
+  gemm_accurate(c, h);  // FP64-level: C carries the small singular directions of the next region
   if (owned) free_tensor(c, M);
   if (spectrum)
     for (int64_t i = 0; i < std::min<int64_t>(spectrum_cap, origm); ++i)

@@ -233,6 +233,20 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   check_launch("gemm_f64_simt");
 }
 
+// FP64-level products: the Ozaki tensor-core form when the split precision is selected,
+// otherwise the FP64 CUDA cores (never TF32x3).
+void gemm_accurate(nsg_ctx* c, const GemmArgs& g_in) {
+  GemmArgs g = g_in;
+  if (g.dtype == NSG_F64) {
+    if (g.opA == OP_C) g.opA = OP_T;
+    if (g.opA == OP_R) g.opA = OP_N;
+    if (g.opB == OP_C) g.opB = OP_T;
+    if (g.opB == OP_R) g.opB = OP_N;
+  }
+  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g)) return;
+  gemm_f64_simt(c, g);
+}
+
 void gemm(nsg_ctx* c, const GemmArgs& g_in) {
   GemmArgs g = g_in;
   if (g.dtype == NSG_F64) {  // conjugation is the identity on real data

@@ -124,6 +124,7 @@ struct GemmArgs {
 // dispatches by the context's precision mode and shape
 void gemm(nsg_ctx* c, const GemmArgs& g);
 void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g);
+void gemm_accurate(nsg_ctx* c, const GemmArgs& g);  // FP64-level: Ozaki or FP64 cores
 bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g);  // TF32x3; false if not applicable
 bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g);  // BF16 multi-slice; false if not applicable
 

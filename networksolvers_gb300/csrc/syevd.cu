@@ -1,12 +1,14 @@
 // Dense Hermitian eigensolver for the truncated factorizations:
 //   1. Householder reduction to a real symmetric tridiagonal T (one cooperative
-//      kernel, two grid barriers per column; the matrix stays L2-resident),
+//      kernel, one grid barrier per column; the matrix stays L2-resident),
 //   2. Cuppen divide and conquer on T: Jacobi leaves of <= 32, rank-one merges with
 //      deflation (small z / close poles), secular roots by bracketed Newton with the
 //      origin at the nearer pole (one thread per root over many CTAs), Gu-Eisenstat
 //      recomputed z for orthogonal vectors, merged by an FP64 GEMM,
 //   3. back-transformation of the kept eigenvectors with the Householder reflectors
-//      in blocks of 32 (compact WY, three GEMMs per block).
+//      in blocks of 128 (compact WY, three GEMMs per block).
+// Every GEMM inside the eigensolver runs on the FP64 cores: with the six-slice Ozaki
+// products the reflector Gram matrix V^H V alone costs 1e-11 of orthogonality.
 // Every wait in these kernels is bounded: the grid barrier gives up after ~2^26
 // polls, raises an error flag and the host reports NSG_ERR_TIMEOUT.
 #include "nsg_internal.h"
@@ -22,7 +24,6 @@ void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* 
 
 namespace {
 
-constexpr int kTriThreads = 256;
 constexpr int kLeaf = 32;
 
 __device__ __forceinline__ double cre(double v) { return v; }
@@ -126,22 +127,23 @@ __device__ T block_sum(T v, T* red) {
 // rebuilds the updated pivot column itself, and one pass over the trailing block both
 // applies the pending update and forms step k's x (one grid barrier per column).  CTAs
 // retire as the trailing block shrinks (the barrier target follows the active count).
-template <typename T>
-__global__ void __launch_bounds__(kTriThreads)
+template <typename T, int NT>
+__global__ void __launch_bounds__(NT)
     tridiag_kernel(T* __restrict__ A, int n, double* __restrict__ d, double* __restrict__ e, T* __restrict__ tau,
-                   T* __restrict__ xbuf, T* __restrict__ partial, Barrier* bar) {
+                   T* __restrict__ xbuf, T* __restrict__ partial, Barrier* bar, int per_thread) {
   extern __shared__ unsigned char smem_raw[];
   T* vprev = (T*)smem_raw;  // pending update (relative to rows >= k)
   T* wprev = vprev + n;
   T* vcur = wprev + n;      // current reflector (relative to rows >= k+1)
-  __shared__ T red[kTriThreads / 32];
-  __shared__ double2 wsum[kTriThreads / 32];
-  const int tid = threadIdx.x, nt = blockDim.x, b = blockIdx.x;
-  const int warp = tid >> 5, lane = tid & 31, nwarps = nt >> 5;
+  __shared__ T red[NT / 32];
+  __shared__ double2 wsum[NT / 32];
+  constexpr int nt = NT, nwarps = NT / 32;
+  const int tid = threadIdx.x, b = blockIdx.x;
+  const int warp = tid >> 5, lane = tid & 31;
   bool has_prev = false;
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;  // trailing size (rows k+1..n-1)
-    int nact = int(((int64_t)m * m + (int64_t)nt * 64 - 1) / ((int64_t)nt * 64));
+    int nact = int(((int64_t)m * m + (int64_t)nt * per_thread - 1) / ((int64_t)nt * per_thread));
     nact = max(1, min(nact, (int)gridDim.x));
     if (b >= nact) return;
     const int gwarp = b * nwarps + warp, gnwarps = nact * nwarps;
@@ -155,14 +157,21 @@ __global__ void __launch_bounds__(kTriThreads)
     const T wp0 = has_prev ? cconj(wprev[0]) : czero<T>();
     const T vp0 = has_prev ? cconj(vprev[0]) : czero<T>();
     auto colval = [&](int i) -> T {  // i >= k
-      T a = colk[i];
+      T a = __ldcg(colk + i);
       if (has_prev) a = csub(a, cadd(cmulv(vprev[i - k], wp0), cmulv(wprev[i - k], vp0)));
       return a;
     };
+    // one read of the pivot column: vcur holds it until the reflector is known
+    T dk = czero<T>();
+    if (b == 0 && tid == 0) dk = colval(k);
     double ss = 0.0;
-    for (int i = k + 2 + tid; i < n; i += nt) ss += cabs2(colval(i));
-    const double xnorm2 = block_sum<double>(ss, (double*)red);
-    const T alpha = colval(k + 1);
+    for (int r = tid; r < m; r += nt) {
+      const T a = colval(k + 1 + r);
+      vcur[r] = a;
+      if (r > 0) ss += cabs2(a);
+    }
+    const double xnorm2 = block_sum<double>(ss, (double*)red);  // its barriers publish vcur
+    const T alpha = vcur[0];
     const double ar = cre(alpha);
     double ai = 0.0;
     if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
@@ -184,10 +193,11 @@ __global__ void __launch_bounds__(kTriThreads)
         scale = *(T*)&s1;
       }
     }
-    for (int r = tid; r < m; r += nt) vcur[r] = (r == 0) ? cone<T>() : cmulv(colval(k + 1 + r), scale);
+    __syncthreads();  // every thread has read vcur[0]
+    for (int r = tid; r < m; r += nt) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scale);
     __syncthreads();
     if (b == 0 && tid == 0) {
-      d[k] = cre(colval(k));
+      d[k] = cre(dk);
       e[k] = active ? beta : ar;
       tau[k] = tk;
     }
@@ -197,31 +207,36 @@ __global__ void __launch_bounds__(kTriThreads)
       T* cj = A + (size_t)(k + 1 + jj) * n + (k + 1);
       const T wj = has_prev ? cconj(wprev[jj + 1]) : czero<T>();
       const T vj = has_prev ? cconj(vprev[jj + 1]) : czero<T>();
-      // four independent loads in flight per lane (the pass is L2-latency bound)
+      // U independent loads in flight per lane (the pass is L2-latency bound); the
+      // trailing block is rewritten by other CTAs between steps, so every access of it
+      // bypasses L1 (ld/st .cg)
+      constexpr int U = sizeof(T) == 8 ? 16 : 8;
       T acc = czero<T>(), acc1 = czero<T>(), acc2 = czero<T>(), acc3 = czero<T>();
       int ii = lane;
-      for (; ii + 96 < m; ii += 128) {
-        T v0 = cj[ii], v1 = cj[ii + 32], v2 = cj[ii + 64], v3 = cj[ii + 96];
+      for (; ii + 32 * (U - 1) < m; ii += 32 * U) {
+        T v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) v[u] = __ldcg(cj + ii + 32 * u);
         if (has_prev) {
-          v0 = csub(v0, cadd(cmulv(vprev[ii + 1], wj), cmulv(wprev[ii + 1], vj)));
-          v1 = csub(v1, cadd(cmulv(vprev[ii + 33], wj), cmulv(wprev[ii + 33], vj)));
-          v2 = csub(v2, cadd(cmulv(vprev[ii + 65], wj), cmulv(wprev[ii + 65], vj)));
-          v3 = csub(v3, cadd(cmulv(vprev[ii + 97], wj), cmulv(wprev[ii + 97], vj)));
-          cj[ii] = v0;
-          cj[ii + 32] = v1;
-          cj[ii + 64] = v2;
-          cj[ii + 96] = v3;
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            v[u] = csub(v[u], cadd(cmulv(vprev[ii + 32 * u + 1], wj), cmulv(wprev[ii + 32 * u + 1], vj)));
+            __stcg(cj + ii + 32 * u, v[u]);
+          }
         }
-        acc = cadd(acc, cmulv(cconj(v0), vcur[ii]));
-        acc1 = cadd(acc1, cmulv(cconj(v1), vcur[ii + 32]));
-        acc2 = cadd(acc2, cmulv(cconj(v2), vcur[ii + 64]));
-        acc3 = cadd(acc3, cmulv(cconj(v3), vcur[ii + 96]));
+#pragma unroll
+        for (int u = 0; u < U; u += 4) {
+          acc = cadd(acc, cmulv(cconj(v[u]), vcur[ii + 32 * u]));
+          acc1 = cadd(acc1, cmulv(cconj(v[u + 1]), vcur[ii + 32 * (u + 1)]));
+          acc2 = cadd(acc2, cmulv(cconj(v[u + 2]), vcur[ii + 32 * (u + 2)]));
+          acc3 = cadd(acc3, cmulv(cconj(v[u + 3]), vcur[ii + 32 * (u + 3)]));
+        }
       }
       for (; ii < m; ii += 32) {
-        T val = cj[ii];
+        T val = __ldcg(cj + ii);
         if (has_prev) {
           val = csub(val, cadd(cmulv(vprev[ii + 1], wj), cmulv(wprev[ii + 1], vj)));
-          cj[ii] = val;
+          __stcg(cj + ii, val);
         }
         acc = cadd(acc, cmulv(cconj(val), vcur[ii]));
       }
@@ -238,7 +253,7 @@ __global__ void __launch_bounds__(kTriThreads)
       }
       if (lane == 0) {
         T xi = cmulv(tk, acc);
-        xb[jj] = xi;
+        __stcg(xb + jj, xi);
         T p = cmulv(cconj(xi), vcur[jj]);
         if constexpr (sizeof(T) == 8) {
           pacc.x += (double&)p;
@@ -256,7 +271,7 @@ __global__ void __launch_bounds__(kTriThreads)
         sacc.x += wsum[w].x;
         sacc.y += wsum[w].y;
       }
-      pb[b] = sacc;
+      __stcg(pb + b, sacc);
     }
     // 3. barrier among the active CTAs
     {
@@ -287,11 +302,21 @@ __global__ void __launch_bounds__(kTriThreads)
       __syncthreads();
       if (!s_ok) return;
     }
-    // 4. w = x + alpha2 v becomes the pending update (relative to rows >= k+1)
+    // 4. w = x + alpha2 v becomes the pending update (relative to rows >= k+1); the
+    // loads of x and of the partials are issued together
+#pragma unroll 4
+    for (int r = tid; r < m; r += nt) wprev[r] = __ldcg(xb + r);
+    // every warp sums the CTAs' partials (lane-strided, then a butterfly: the same value
+    // in every lane of every CTA)
     double2 xv = make_double2(0.0, 0.0);
-    for (int q = 0; q < nact; ++q) {
-      xv.x += pb[q].x;
-      xv.y += pb[q].y;
+    for (int q = lane; q < nact; q += 32) {
+      const double2 t = __ldcg(pb + q);
+      xv.x += t.x;
+      xv.y += t.y;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      xv.x += __shfl_xor_sync(0xffffffffu, xv.x, o);
+      xv.y += __shfl_xor_sync(0xffffffffu, xv.y, o);
     }
     T xvT;
     if constexpr (sizeof(T) == 8) {
@@ -306,9 +331,9 @@ __global__ void __launch_bounds__(kTriThreads)
     if (b == 0)
       for (int r = tid + 1; r < m; r += nt) A[(size_t)k * n + (k + 1 + r)] = vcur[r];
     __syncthreads();
-    for (int r = tid; r < m; r += nt) {
+    for (int r = tid; r < m; r += nt) {  // the entries this thread loaded above
       vprev[r] = vcur[r];
-      wprev[r] = active ? cadd(xb[r], cmulv(alpha2, vcur[r])) : czero<T>();
+      wprev[r] = active ? cadd(wprev[r], cmulv(alpha2, vcur[r])) : czero<T>();
     }
     has_prev = active;
     __syncthreads();
@@ -316,7 +341,7 @@ __global__ void __launch_bounds__(kTriThreads)
   if (b == 0 && tid == 0) {
     // last 2 x 2 block with the pending update of step n-3 (relative to rows >= n-2)
     auto upd = [&](int i, int j) -> T {
-      T a = A[i + (size_t)j * n];
+      T a = __ldcg(A + i + (size_t)j * n);
       if (has_prev && n >= 3)
         a = csub(a, cadd(cmulv(vprev[i - (n - 2)], cconj(wprev[j - (n - 2)])),
                          cmulv(wprev[i - (n - 2)], cconj(vprev[j - (n - 2)]))));
@@ -777,25 +802,24 @@ __global__ void scale_rows_phase_kernel(double2* Z, int64_t rows, int64_t cols, 
   }
 }
 
-// compact WY: T factor (upper triangular, nbk x nbk <= 32) for reflectors k0..k0+nbk-1
-// from S = V^H V: T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] S[0:j, j]; lane i owns row i.
+// compact WY: T factor (upper triangular, nbk x nbk <= 128) for reflectors
+// k0..k0+nbk-1 from S = V^H V: T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] S[0:j, j];
+// one CTA, thread i owns row i.
 template <typename T>
 __global__ void wy_tfactor_kernel(const T* S, int nbk, const T* tau, T* Tm) {
   const int i = threadIdx.x;
-  if (blockIdx.x != 0 || i >= 32) return;
-  for (int j = 0; j < nbk; ++j) {
+  if (blockIdx.x != 0) return;
+  for (int j = 0; j < nbk; ++j)
     if (i < nbk) Tm[i + j * nbk] = czero<T>();
-  }
-  __syncwarp();
+  __syncthreads();
   for (int j = 0; j < nbk; ++j) {
-    T tj = tau[j];
     T acc = czero<T>();
     if (i < j)
       for (int l = i; l < j; ++l) acc = cadd(acc, cmulv(Tm[i + l * nbk], S[l + j * nbk]));
-    __syncwarp();
-    if (i < j) Tm[i + j * nbk] = cscale(cmulv(tj, acc), -1.0);
-    if (i == j) Tm[j + j * nbk] = tj;
-    __syncwarp();
+    __syncthreads();
+    if (i < j) Tm[i + j * nbk] = cscale(cmulv(tau[j], acc), -1.0);
+    if (i == j) Tm[j + j * nbk] = tau[j];
+    __syncthreads();
   }
 }
 
@@ -970,10 +994,10 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
 
 template <typename T>
 static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* tau_dev, T* Z, int64_t ldz, int64_t k) {
-  // Z <- H_0 H_1 ... H_{n-3} Z, blocks of 32 reflectors applied last block first
+  // Z <- H_0 H_1 ... H_{n-3} Z, blocks of 128 reflectors applied last block first
   const int nref = n - 2;
   if (nref <= 0 || k == 0) return;
-  const int NB = 32;
+  const int NB = 128;
   const size_t eb = sizeof(T);
   DevBuf V(c, eb * (size_t)n * NB), S(c, eb * NB * NB), Tm(c, eb * NB * NB), Wt(c, eb * (size_t)NB * k),
       W2(c, eb * (size_t)NB * k);
@@ -1000,7 +1024,7 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
     g.C = S.p;
     g.ldc = nbk;
     gemm_f64_simt(c, g);
-    wy_tfactor_kernel<T><<<1, 32, 0, c->stream>>>(S.as<T>(), nbk, tau_dev + k0, Tm.as<T>());
+    wy_tfactor_kernel<T><<<1, 128, 0, c->stream>>>(S.as<T>(), nbk, tau_dev + k0, Tm.as<T>());
     count_launch(c);
     // W = V^H Z(rows k0+1..)  (nbk x k)
     GemmArgs h = g;
@@ -1070,8 +1094,12 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
     int max_blocks = 0;
     size_t shm = eb * 3 * n;
     NSG_CHECK(shm <= 200 * 1024, NSG_ERR_UNSUPPORTED, "tridiagonalisation: matrix order too large");
-    NSG_CUDA(cudaFuncSetAttribute(tridiag_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
-    NSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks, tridiag_kernel<T>, kTriThreads, shm));
+    // one CTA of 256 threads per SM: the active CTAs (the first nact block indices) are
+    // then spread over all SMs; wider CTAs and two CTAs per SM measured slower
+    constexpr int kTriThreads = 256;
+    auto kfn = tridiag_kernel<T, kTriThreads>;
+    NSG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    NSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks, kfn, kTriThreads, shm));
     NSG_CHECK(max_blocks > 0, NSG_ERR_UNSUPPORTED, "tridiagonalisation: no resident block fits");
     int64_t want = ((int64_t)n * n + kTriThreads * 8 - 1) / (kTriThreads * 8);
     int grid = int(std::min<int64_t>({(int64_t)max_blocks * c->num_sms, std::max<int64_t>(want, 1),
@@ -1084,9 +1112,10 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
     T* px = xbuf.as<T>();
     T* pp = part.as<T>();
     Barrier* pb = bar.as<Barrier>();
-    void* args[] = {&A, &n, &pd, &pe, &pt, &px, &pp, &pb};
+    int pt_arg = 4;  // trailing elements per thread before another CTA joins the pass
+    void* args[] = {&A, &n, &pd, &pe, &pt, &px, &pp, &pb, &pt_arg};
     ProfScope ps(c, NSG_PROF_TRIDIAG, (sizeof(T) == 16 ? 16.0 : 4.0) / 3.0 * double(n) * n * n);
-    NSG_CUDA(cudaLaunchCooperativeKernel((void*)tridiag_kernel<T>, dim3(grid), dim3(kTriThreads), args, shm,
+    NSG_CUDA(cudaLaunchCooperativeKernel((void*)kfn, dim3(grid), dim3(kTriThreads), args, shm,
                                          c->stream));
     count_launch(c);
     check_launch("tridiag");

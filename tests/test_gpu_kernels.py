@@ -266,15 +266,22 @@ def _dmrg_like(rng, m, n, cplx):
     return (U * s) @ V.conj().T
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
 @pytest.mark.parametrize("cplx", [False, True])
 @pytest.mark.parametrize("m,n", [(1, 3), (33, 33), (64, 40), (200, 260), (513, 513), (1100, 900)])
-def test_eigensolver_large_and_degenerate(nsg_ctx, cplx, m, n):
+def test_eigensolver_large_and_degenerate(nsg_ctx, cplx, m, n, precision):
+    """Exact bond dimensions, orthonormal U (1e-12) and the discarded weight, in the plain
+    form and with C = U^H M on the Ozaki tensor-core path."""
     rng = np.random.default_rng(m + 7 * n)
     M = _dmrg_like(rng, m, n, cplx)
     l, r = Index(m), Index(n)
     T = DTensor.from_numpy(M, [l, r])
     for cutoff, maxdim in [(0.0, None), (1e-12, None), (1e-8, 3 * min(m, n) // 4 + 1)]:
-        U, Cc, info = it.factorize(T, [l], cutoff=cutoff, maxdim=maxdim, spectrum=True)
+        nsg_ctx.set_precision(precision)
+        try:
+            U, Cc, info = it.factorize(T, [l], cutoff=cutoff, maxdim=maxdim, spectrum=True)
+        finally:
+            nsg_ctx.set_precision("fp64")
         s = np.linalg.svd(M, compute_uv=False)
         kref, errref = ol.truncate_spectrum(s ** 2, cutoff, maxdim)
         assert info["newdim"] == kref, (cutoff, maxdim)
