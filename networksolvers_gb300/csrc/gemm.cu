@@ -233,8 +233,9 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   check_launch("gemm_f64_simt");
 }
 
-// FP64-level products: the Ozaki tensor-core form when the split precision is selected,
-// otherwise the FP64 CUDA cores (never TF32x3).
+// FP64-level products: the eight-slice Ozaki tensor-core form (2^-55 of the row and
+// column scales) when the split precision is selected, otherwise the FP64 CUDA cores
+// (never TF32x3).
 void gemm_accurate(nsg_ctx* c, const GemmArgs& g_in) {
   GemmArgs g = g_in;
   if (g.dtype == NSG_F64) {
@@ -243,7 +244,7 @@ void gemm_accurate(nsg_ctx* c, const GemmArgs& g_in) {
     if (g.opB == OP_C) g.opB = OP_T;
     if (g.opB == OP_R) g.opB = OP_N;
   }
-  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g)) return;
+  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g, 8)) return;
   gemm_f64_simt(c, g);
 }
 
@@ -262,7 +263,7 @@ void gemm(nsg_ctx* c, const GemmArgs& g_in) {
     return;
   }
   if (c->precision == NSG_PREC_TF32X3 && gemm_split_tc(c, g)) return;
-  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g)) return;
+  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g, 8)) return;
   gemm_f64_simt(c, g);
 }
 

@@ -31,17 +31,24 @@ namespace nsg {
 
 namespace {
 
-constexpr int S = 6;                 // slices per operand
-constexpr int G = S;                 // groups g = s + t in [0, S-1]
 constexpr int BM = 128, BN = 64, BKS = 32;  // K slab: 32 bf16 = 64 bytes
-constexpr int STAGES = 3;
 constexpr int SLICE_A = BM * BKS * 2;       // 8 KB
 constexpr int SLICE_B = BN * BKS * 2;       // 4 KB
-constexpr int STAGE_BYTES = S * (SLICE_A + SLICE_B);  // 72 KB
 constexpr int CHUNK_SLABS = 4;              // K = 128 per exact chunk
 constexpr int NDRAIN_WARPS = 16;
 constexpr int NTHREADS = (NDRAIN_WARPS + 1) * 32;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;
+
+// S slices per operand, groups g = s + t in [0, S-1] (G x 64 TMEM columns <= 512);
+// S = 8 fills TMEM and leaves room for two 96 KB stages of shared memory.
+template <int S_>
+struct Oz {
+  static constexpr int S = S_, G = S_;
+  static constexpr int STAGES = S_ <= 6 ? 3 : 2;
+  static constexpr int STAGE_BYTES = S * (SLICE_A + SLICE_B);
+  static constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 512;
+  static_assert(G * BN <= 512, "accumulators exceed TMEM");
+  static_assert(SMEM_BYTES <= 227 * 1024, "stages exceed shared memory");
+};
 constexpr long long kWaitLimit = 1ll << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -126,6 +133,7 @@ __global__ void row_scale_kernel(const double* __restrict__ src, int64_t rows, i
 }
 
 // slices: out[(b*S + s)][r][k] (bf16, K-major, padded with zeros)
+template <int S>
 __global__ void slice_kernel(const double* __restrict__ src, int64_t rows, int64_t K, int64_t rs, int64_t ks,
                              int64_t bs, int64_t rows_p, int64_t K_p, const double* __restrict__ scale,
                              __nv_bfloat16* __restrict__ out, int64_t batch) {
@@ -182,9 +190,11 @@ __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   lo += e;
 }
 
+template <int S_>
 __global__ void __launch_bounds__(NTHREADS, 1)
     oz_gemm_kernel(const __grid_constant__ CUtensorMap mapA, const __grid_constant__ CUtensorMap mapB, int nk,
                    OzEpi ep) {
+  constexpr int S = Oz<S_>::S, G = Oz<S_>::G, STAGES = Oz<S_>::STAGES, STAGE_BYTES = Oz<S_>::STAGE_BYTES;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   uint64_t* full = (uint64_t*)(smem + STAGES * STAGE_BYTES);
@@ -361,7 +371,7 @@ EncodeFn encode_fn() {
 }
 
 // slices [planes = batch*S][rows_p][K_p] bf16; box {32, box_rows, S}
-CUtensorMap make_map(void* base, int64_t rows_p, int64_t K_p, int64_t planes, int box_rows) {
+CUtensorMap make_map(void* base, int64_t rows_p, int64_t K_p, int64_t planes, int box_rows, int S) {
   EncodeFn enc = encode_fn();
   NSG_CHECK(enc != nullptr, NSG_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
   CUtensorMap m;
@@ -376,6 +386,7 @@ CUtensorMap make_map(void* base, int64_t rows_p, int64_t K_p, int64_t planes, in
   return m;
 }
 
+template <int S>
 void slice_operand(nsg_ctx* c, const double* src, int64_t rows, int64_t K, int64_t rs, int64_t ks, int64_t bs,
                    int64_t batch, int64_t rows_p, int64_t K_p, double* scale, __nv_bfloat16* out) {
   {
@@ -387,14 +398,14 @@ void slice_operand(nsg_ctx* c, const double* src, int64_t rows, int64_t K, int64
   int64_t ntiles = (rows_p / 32) * (K_p / 32) * batch;
   int grid = int(std::min<int64_t>(ntiles, (int64_t)c->num_sms * 16));
   ProfScope ps(c, NSG_PROF_SPLIT, 0.0);
-  slice_kernel<<<grid, 256, 0, c->stream>>>(src, rows, K, rs, ks, bs, rows_p, K_p, scale, out, batch);
+  slice_kernel<S><<<grid, 256, 0, c->stream>>>(src, rows, K, rs, ks, bs, rows_p, K_p, scale, out, batch);
   count_launch(c, 2);
   check_launch("ozaki slices");
 }
 
-}  // namespace
-
-bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g) {
+template <int S>
+bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
+  constexpr int SMEM_BYTES = Oz<S>::SMEM_BYTES;
   if (g.dtype != NSG_F64) return false;
   if (g.opA == OP_C || g.opA == OP_R || g.opB == OP_C || g.opB == OP_R) return false;
   if (g.M < 64 || g.N < 32 || g.K < 64) return false;
@@ -410,14 +421,14 @@ bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g) {
   __nv_bfloat16* Bs = As + nA;
   double* sa = (double*)(((uintptr_t)(Bs + nB) + 255) & ~(uintptr_t)255);
   double* sb = sa + Mp * ab;
-  slice_operand(c, (const double*)g.A, g.M, g.K, ars, aks, g.strideA, ab, Mp, Kp, sa, As);
-  slice_operand(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
-  CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM), mB = make_map(Bs, Np, Kp, S * bb, BN);
+  slice_operand<S>(c, (const double*)g.A, g.M, g.K, ars, aks, g.strideA, ab, Mp, Kp, sa, As);
+  slice_operand<S>(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
+  CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM, S), mB = make_map(Bs, Np, Kp, S * bb, BN, S);
   int* err = (int*)dev_scratch(c, 1);
   NSG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-  static bool attr = false;
+  static bool attr = false;  // one flag per instantiation
   if (!attr) {
-    NSG_CUDA(cudaFuncSetAttribute(oz_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    NSG_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr = true;
   }
   OzEpi ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, sa, sb, Mp, Np,
@@ -425,7 +436,7 @@ bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g) {
   dim3 grid(unsigned(Mp / BM), unsigned(Np / BN), unsigned(g.batch));
   {
     ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(g.M) * double(g.N) * double(g.K) * double(g.batch));
-    oz_gemm_kernel<<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, int(Kp / BKS), ep);
+    oz_gemm_kernel<S><<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, int(Kp / BKS), ep);
   }
   count_launch(c);
   check_launch("oz_gemm");
@@ -435,6 +446,13 @@ bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g) {
   NSG_CUDA(cudaStreamSynchronize(c->stream));
   NSG_CHECK(herr == 0, NSG_ERR_TIMEOUT, "oz_gemm: a bounded mbarrier wait timed out");
   return true;
+}
+
+}  // namespace
+
+bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g, int slices) {
+  if (slices == 8) return gemm_ozaki_impl<8>(c, g);
+  return gemm_ozaki_impl<6>(c, g);
 }
 
 }  // namespace nsg

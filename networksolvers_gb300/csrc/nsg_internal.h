@@ -126,7 +126,7 @@ void gemm(nsg_ctx* c, const GemmArgs& g);
 void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g);
 void gemm_accurate(nsg_ctx* c, const GemmArgs& g);  // FP64-level: Ozaki or FP64 cores
 bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g);  // TF32x3; false if not applicable
-bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g);  // BF16 multi-slice; false if not applicable
+bool gemm_ozaki_tc(nsg_ctx* c, const GemmArgs& g, int slices = 6);  // BF16 6 or 8 slices; false if not applicable
 
 void permute(nsg_ctx* c, const nsg_tensor* x, const int* perm, bool conj, nsg_tensor* out);
 void axpby(nsg_ctx* c, int dtype, int64_t n, double ar, double ai, const void* x, double br,

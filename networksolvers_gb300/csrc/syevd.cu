@@ -7,8 +7,10 @@
 //      recomputed z for orthogonal vectors, merged by an FP64 GEMM,
 //   3. back-transformation of the kept eigenvectors with the Householder reflectors
 //      in blocks of 128 (compact WY, three GEMMs per block).
-// Every GEMM inside the eigensolver runs on the FP64 cores: with the six-slice Ozaki
-// products the reflector Gram matrix V^H V alone costs 1e-11 of orthogonality.
+// The merge GEMMs and the two large back-transformation GEMMs use the FP64-level
+// products (eight-slice Ozaki form in the split precision); the reflector Gram matrix
+// V^H V and T W stay on the FP64 cores (six-slice products there alone cost 1e-11 of
+// orthogonality).
 // Every wait in these kernels is bounded: the grid barrier gives up after ~2^26
 // polls, raises an error flag and the host reports NSG_ERR_TIMEOUT.
 #include "nsg_internal.h"
@@ -25,6 +27,7 @@ void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* 
 namespace {
 
 constexpr int kLeaf = 32;
+constexpr int kTriUnits = 1024;  // pass work units per CTA and step (columns x row blocks)
 
 __device__ __forceinline__ double cre(double v) { return v; }
 __device__ __forceinline__ double cre(double2 v) { return v.x; }
@@ -58,6 +61,21 @@ __device__ __forceinline__ double cdiv(double a, double b) { return a / b; }
 __device__ __forceinline__ double2 cdiv(double2 a, double2 b) {
   double den = b.x * b.x + b.y * b.y;
   return make_double2((a.x * b.x + a.y * b.y) / den, (a.y * b.x - a.x * b.y) / den);
+}
+
+// v - a b - c d and acc + conj(a) b as chains of fused multiply-adds (two FP64
+// operations per real element: the FP64 pipe bounds the tridiagonalisation)
+__device__ __forceinline__ double fnms2(double v, double a, double b, double c, double d) {
+  return fma(-c, d, fma(-a, b, v));
+}
+__device__ __forceinline__ double2 fnms2(double2 v, double2 a, double2 b, double2 c, double2 d) {
+  double re = fma(c.y, d.y, fma(-c.x, d.x, fma(a.y, b.y, fma(-a.x, b.x, v.x))));
+  double im = fma(-c.y, d.x, fma(-c.x, d.y, fma(-a.y, b.x, fma(-a.x, b.y, v.y))));
+  return make_double2(re, im);
+}
+__device__ __forceinline__ double fcma(double acc, double a, double b) { return fma(a, b, acc); }
+__device__ __forceinline__ double2 fcma(double2 acc, double2 a, double2 b) {
+  return make_double2(fma(a.y, b.y, fma(a.x, b.x, acc.x)), fma(-a.y, b.x, fma(a.x, b.y, acc.y)));
 }
 
 // Grid barrier with a bounded wait (cooperative launch guarantees co-residency).
@@ -137,6 +155,7 @@ __global__ void __launch_bounds__(NT)
   T* vcur = wprev + n;      // current reflector (relative to rows >= k+1)
   __shared__ T red[NT / 32];
   __shared__ double2 wsum[NT / 32];
+  __shared__ T part_s[kTriUnits];  // per-unit partial dot products of the pass
   constexpr int nt = NT, nwarps = NT / 32;
   const int tid = threadIdx.x, b = blockIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
@@ -146,7 +165,6 @@ __global__ void __launch_bounds__(NT)
     int nact = int(((int64_t)m * m + (int64_t)nt * per_thread - 1) / ((int64_t)nt * per_thread));
     nact = max(1, min(nact, (int)gridDim.x));
     if (b >= nact) return;
-    const int gwarp = b * nwarps + warp, gnwarps = nact * nwarps;
     // x and the partial sums are double-buffered by step parity: a CTA that runs ahead
     // writes the other buffer while a slower one still reads this step's values (the
     // barrier keeps every CTA within one step of the others)
@@ -158,7 +176,7 @@ __global__ void __launch_bounds__(NT)
     const T vp0 = has_prev ? cconj(vprev[0]) : czero<T>();
     auto colval = [&](int i) -> T {  // i >= k
       T a = __ldcg(colk + i);
-      if (has_prev) a = csub(a, cadd(cmulv(vprev[i - k], wp0), cmulv(wprev[i - k], vp0)));
+      if (has_prev) a = fnms2(a, vprev[i - k], wp0, wprev[i - k], vp0);
       return a;
     };
     // one read of the pivot column: vcur holds it until the reflector is known
@@ -201,60 +219,72 @@ __global__ void __launch_bounds__(NT)
       e[k] = active ? beta : ar;
       tau[k] = tk;
     }
-    // 2. one pass over the trailing block: pending update, then x_j = tau * A22[:, j]^H v
-    double2 pacc = make_double2(0.0, 0.0);
-    for (int jj = gwarp; jj < m; jj += gnwarps) {
-      T* cj = A + (size_t)(k + 1 + jj) * n + (k + 1);
-      const T wj = has_prev ? cconj(wprev[jj + 1]) : czero<T>();
-      const T vj = has_prev ? cconj(vprev[jj + 1]) : czero<T>();
-      // U independent loads in flight per lane (the pass is L2-latency bound); the
-      // trailing block is rewritten by other CTAs between steps, so every access of it
-      // bypasses L1 (ld/st .cg)
-      constexpr int U = sizeof(T) == 8 ? 16 : 8;
-      T acc = czero<T>(), acc1 = czero<T>(), acc2 = czero<T>(), acc3 = czero<T>();
-      int ii = lane;
-      for (; ii + 32 * (U - 1) < m; ii += 32 * U) {
-        T v[U];
+    // 2. the CTA's columns [j0, j1) of the trailing block: pending update, then
+    //    x_j = tau * A22[:, j]^H v.  Work units (one column x RB rows) are dealt to the
+    //    warps round-robin, so the warps carry equal loads; a warp loads its next unit
+    //    before it updates and stores the current one (units are disjoint).  The trailing
+    //    block is rewritten by other CTAs between steps: every access bypasses L1.
+    {
+      constexpr int U = sizeof(T) == 8 ? 16 : 8, RB = 32 * U;
+      const int j0 = int((int64_t)m * b / nact), j1 = int((int64_t)m * (b + 1) / nact);
+      const int ncol = j1 - j0, nrb = (m + RB - 1) / RB, nunits = ncol * nrb;
+      T cur[U], nxt[U];
+      auto load_unit = [&](int u, T* dst) {
+        const int q = u / nrb, rb = u - q * nrb;
+        const T* cj = A + (size_t)(k + 1 + j0 + q) * n + (k + 1);
 #pragma unroll
-        for (int u = 0; u < U; ++u) v[u] = __ldcg(cj + ii + 32 * u);
-        if (has_prev) {
+        for (int t = 0; t < U; ++t) {
+          const int r = rb * RB + 32 * t + lane;
+          dst[t] = r < m ? __ldcg(cj + r) : czero<T>();
+        }
+      };
+      if (warp < nunits) load_unit(warp, cur);
+      for (int u = warp; u < nunits; u += nwarps) {
+        if (u + nwarps < nunits) load_unit(u + nwarps, nxt);
+        const int q = u / nrb, rb = u - q * nrb, jj = j0 + q;
+        T* cj = A + (size_t)(k + 1 + jj) * n + (k + 1);
+        const T wj = has_prev ? cconj(wprev[jj + 1]) : czero<T>();
+        const T vj = has_prev ? cconj(vprev[jj + 1]) : czero<T>();
+        T acc = czero<T>(), acc1 = czero<T>();
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
-            v[u] = csub(v[u], cadd(cmulv(vprev[ii + 32 * u + 1], wj), cmulv(wprev[ii + 32 * u + 1], vj)));
-            __stcg(cj + ii + 32 * u, v[u]);
+        for (int t = 0; t < U; ++t) {
+          const int r = rb * RB + 32 * t + lane;
+          if (r < m) {
+            T val = cur[t];
+            if (has_prev) {
+              val = fnms2(val, vprev[r + 1], wj, wprev[r + 1], vj);
+              __stcg(cj + r, val);
+            }
+            if (t & 1)
+              acc1 = fcma(acc1, val, vcur[r]);
+            else
+              acc = fcma(acc, val, vcur[r]);
           }
         }
+        acc = cadd(acc, acc1);
+        for (int o = 16; o > 0; o >>= 1) {
+          if constexpr (sizeof(T) == 8) {
+            acc += __shfl_down_sync(0xffffffffu, acc, o);
+          } else {
+            double2 t2;
+            t2.x = __shfl_down_sync(0xffffffffu, ((double2&)acc).x, o);
+            t2.y = __shfl_down_sync(0xffffffffu, ((double2&)acc).y, o);
+            acc = cadd(acc, *(T*)&t2);
+          }
+        }
+        if (lane == 0) part_s[u] = acc;
 #pragma unroll
-        for (int u = 0; u < U; u += 4) {
-          acc = cadd(acc, cmulv(cconj(v[u]), vcur[ii + 32 * u]));
-          acc1 = cadd(acc1, cmulv(cconj(v[u + 1]), vcur[ii + 32 * (u + 1)]));
-          acc2 = cadd(acc2, cmulv(cconj(v[u + 2]), vcur[ii + 32 * (u + 2)]));
-          acc3 = cadd(acc3, cmulv(cconj(v[u + 3]), vcur[ii + 32 * (u + 3)]));
-        }
+        for (int t = 0; t < U; ++t) cur[t] = nxt[t];
       }
-      for (; ii < m; ii += 32) {
-        T val = __ldcg(cj + ii);
-        if (has_prev) {
-          val = csub(val, cadd(cmulv(vprev[ii + 1], wj), cmulv(wprev[ii + 1], vj)));
-          __stcg(cj + ii, val);
-        }
-        acc = cadd(acc, cmulv(cconj(val), vcur[ii]));
-      }
-      acc = cadd(cadd(acc, acc1), cadd(acc2, acc3));
-      for (int o = 16; o > 0; o >>= 1) {
-        if constexpr (sizeof(T) == 8) {
-          acc += __shfl_down_sync(0xffffffffu, acc, o);
-        } else {
-          double2 t;
-          t.x = __shfl_down_sync(0xffffffffu, ((double2&)acc).x, o);
-          t.y = __shfl_down_sync(0xffffffffu, ((double2&)acc).y, o);
-          acc = cadd(acc, *(T*)&t);
-        }
-      }
-      if (lane == 0) {
-        T xi = cmulv(tk, acc);
-        __stcg(xb + jj, xi);
-        T p = cmulv(cconj(xi), vcur[jj]);
+      __syncthreads();
+      // column sums in a fixed order, x, and this CTA's share of x^H v
+      double2 pacc = make_double2(0.0, 0.0);
+      for (int q = tid; q < ncol; q += nt) {
+        T sum = czero<T>();
+        for (int rb = 0; rb < nrb; ++rb) sum = cadd(sum, part_s[q * nrb + rb]);
+        const T xi = cmulv(tk, sum);
+        __stcg(xb + j0 + q, xi);
+        const T p = cmulv(cconj(xi), vcur[j0 + q]);
         if constexpr (sizeof(T) == 8) {
           pacc.x += (double&)p;
         } else {
@@ -262,16 +292,20 @@ __global__ void __launch_bounds__(NT)
           pacc.y += ((double2&)p).y;
         }
       }
-    }
-    if (lane == 0) wsum[warp] = pacc;
-    __syncthreads();
-    if (tid == 0) {
-      double2 sacc = make_double2(0.0, 0.0);
-      for (int w = 0; w < nwarps; ++w) {
-        sacc.x += wsum[w].x;
-        sacc.y += wsum[w].y;
+      for (int o = 16; o > 0; o >>= 1) {
+        pacc.x += __shfl_down_sync(0xffffffffu, pacc.x, o);
+        pacc.y += __shfl_down_sync(0xffffffffu, pacc.y, o);
       }
-      __stcg(pb + b, sacc);
+      if (lane == 0) wsum[warp] = pacc;
+      __syncthreads();
+      if (tid == 0) {
+        double2 sacc = make_double2(0.0, 0.0);
+        for (int w = 0; w < nwarps; ++w) {
+          sacc.x += wsum[w].x;
+          sacc.y += wsum[w].y;
+        }
+        __stcg(pb + b, sacc);
+      }
     }
     // 3. barrier among the active CTAs
     {
@@ -977,7 +1011,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
         g.ldc = nb;
         g.batch = 1;
         g.strideA = g.strideB = g.strideC = 0;
-        gemm_f64_simt(c, g);
+        gemm_accurate(c, g);
       }
       DevBuf skind(c, sizeof(int) * nb), sidx(c, sizeof(int) * nb), wnew(c, sizeof(double) * nb),
           Qnew(c, sizeof(double) * (size_t)nb * nb);
@@ -1039,7 +1073,7 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
     h.opB = OP_N;
     h.C = Wt.p;
     h.ldc = nbk;
-    gemm_f64_simt(c, h);
+    gemm_accurate(c, h);
     // W2 = T W
     GemmArgs t2 = g;
     t2.M = nbk;
@@ -1069,7 +1103,7 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
     u.ldc = ldz;
     u.alpha_re = -1.0;
     u.beta_re = 1.0;
-    gemm_f64_simt(c, u);
+    gemm_accurate(c, u);
   }
   check_launch("back_transform");
 }
@@ -1104,6 +1138,11 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
     int64_t want = ((int64_t)n * n + kTriThreads * 8 - 1) / (kTriThreads * 8);
     int grid = int(std::min<int64_t>({(int64_t)max_blocks * c->num_sms, std::max<int64_t>(want, 1),
                                       (int64_t)c->num_sms}));
+    {
+      const int64_t rb = sizeof(T) == 8 ? 512 : 256, m = n - 1;
+      const int64_t units = ((m + grid - 1) / grid) * ((m + rb - 1) / rb);
+      NSG_CHECK(units <= kTriUnits, NSG_ERR_UNSUPPORTED, "tridiagonalisation: matrix order too large for the grid");
+    }
     DevBuf xbuf(c, eb * 2 * n), part(c, sizeof(double2) * 2 * grid), bar(c, sizeof(Barrier));
     NSG_CUDA(cudaMemsetAsync(bar.p, 0, sizeof(Barrier), c->stream));
     double* pd = dd.as<double>();
