@@ -75,6 +75,27 @@ double* host_scalars(nsg_ctx* c, size_t n) {
   return c->host_scalars;
 }
 
+int* device_flag(nsg_ctx* c) {
+  if (!c->dev_flag) {
+    NSG_CUDA(cudaMalloc(&c->dev_flag, sizeof(int)));
+    NSG_CUDA(cudaMemsetAsync(c->dev_flag, 0, sizeof(int), c->stream));
+  }
+  c->flag_pending = true;
+  return c->dev_flag;
+}
+
+void check_device_flag(nsg_ctx* c) {
+  if (!c || !c->flag_pending) return;
+  c->flag_pending = false;
+  int h = 0;
+  NSG_CUDA(cudaMemcpyAsync(&h, c->dev_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  if (h) {
+    NSG_CUDA(cudaMemsetAsync(c->dev_flag, 0, sizeof(int), c->stream));
+    throw Error(NSG_ERR_TIMEOUT, "a tensor-core kernel's bounded mbarrier wait timed out");
+  }
+}
+
 double* dev_scratch(nsg_ctx* c, size_t n) {
   if (n > c->dev_scratch_cap) {
     if (c->dev_scratch) {
@@ -133,6 +154,7 @@ int nsg_ctx_destroy(nsg_ctx* c) {
     if (e) cudaEventDestroy(e);
   if (c->host_scalars) cudaFreeHost(c->host_scalars);
   if (c->dev_scratch) cudaFree(c->dev_scratch);
+  if (c->dev_flag) cudaFree(c->dev_flag);
   cudaStreamDestroy(c->stream);
   delete c;
   return NSG_OK;

@@ -169,10 +169,84 @@ __global__ void splitk_reduce_kernel(int64_t M, int64_t N, int64_t batch, int sp
   }
 }
 
+// Tall-skinny products with N, K <= 32 (the site-operator step of H_eff: M = chi, K and N
+// = w d^2, batched over the other bond): one thread per row of C, op(B) staged in
+// shared memory, exactly M N K multiply-adds (the 64x64 tile kernel would pad N and K).
+template <typename T>
+__global__ void __launch_bounds__(256, 1)
+    gemm_skinny_kernel(int64_t M, int N, int K, const T* __restrict__ A, int64_t lda, int64_t sA, bool conjA,
+                       const T* __restrict__ B, int64_t ldb, int64_t sB, int opB, T* __restrict__ C,
+                       int64_t ldc, int64_t sC, int64_t batch, Scal<T> sc) {
+  __shared__ T Bs[32][33];
+  const bool transB = (opB == OP_T || opB == OP_C), conjB = (opB == OP_C || opB == OP_R);
+  for (int64_t bz = blockIdx.y; bz < batch; bz += gridDim.y) {
+    __syncthreads();
+    const T* Bb = B + bz * sB;
+    for (int e = threadIdx.x; e < K * N; e += blockDim.x) {
+      const int k = e % K, j = e / K;
+      Bs[k][j] = ld(transB ? Bb + j + (int64_t)k * ldb : Bb + k + (int64_t)j * ldb, conjB);
+    }
+    __syncthreads();
+    const T* Ab = A + bz * sA;
+    T* Cb = C + bz * sC;
+    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < M; i += int64_t(gridDim.x) * blockDim.x) {
+      T acc[32];
+#pragma unroll
+      for (int j = 0; j < 32; ++j) zero(acc[j]);
+      // eight rows of op(A) in flight per thread (the loads, not the FP64 work, set the
+      // latency of this kernel)
+      for (int k0 = 0; k0 < K; k0 += 8) {
+        T a[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          zero(a[u]);
+          if (k0 + u < K) a[u] = ld(Ab + i + (int64_t)(k0 + u) * lda, conjA);
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (k0 + u < K)
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if (j < N) mac(acc[j], a[u], Bs[k0 + u][j]);
+      }
+#pragma unroll
+      for (int j = 0; j < 32; ++j)
+        if (j < N) {
+          T* cp = Cb + i + (int64_t)j * ldc;
+          *cp = sc.epi(acc[j], cp);
+        }
+    }
+  }
+}
+
 }  // namespace
 
 void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   if (g.M == 0 || g.N == 0 || g.batch == 0) return;
+  if (g.N <= 32 && g.K <= 32 && g.K >= 1 && (g.opA == OP_N || g.opA == OP_R)) {
+    const int64_t sms = c->num_sms > 0 ? c->num_sms : 152;
+    const int64_t rows_blocks = (g.M + 255) / 256;
+    const int64_t gb = std::min<int64_t>(g.batch, 65535);
+    const int64_t gx = std::max<int64_t>(1, std::min<int64_t>(rows_blocks, (sms * 8 + gb - 1) / gb));
+    dim3 grid{unsigned(gx), unsigned(gb), 1};
+    ProfScope ps(c, NSG_PROF_SIMT_GEMM,
+                 double(g.M) * double(g.N) * double(g.K) * double(g.batch) * (g.dtype == NSG_C128 ? 8.0 : 2.0));
+    if (g.dtype == NSG_C128) {
+      Scal<double2> sc{make_double2(g.alpha_re, g.alpha_im), make_double2(g.beta_re, g.beta_im)};
+      gemm_skinny_kernel<double2><<<grid, 256, 0, c->stream>>>(
+          g.M, int(g.N), int(g.K), (const double2*)g.A, g.lda, g.strideA, g.opA == OP_R, (const double2*)g.B,
+          g.ldb, g.strideB, g.opB, (double2*)g.C, g.ldc, g.strideC, g.batch, sc);
+    } else {
+      Scal<double> sc{g.alpha_re, g.beta_re};
+      gemm_skinny_kernel<double><<<grid, 256, 0, c->stream>>>(g.M, int(g.N), int(g.K), (const double*)g.A, g.lda,
+                                                              g.strideA, false, (const double*)g.B, g.ldb,
+                                                              g.strideB, g.opB, (double*)g.C, g.ldc, g.strideC,
+                                                              g.batch, sc);
+    }
+    count_launch(c);
+    check_launch("gemm_skinny");
+    return;
+  }
   int64_t gx = (g.M + BM - 1) / BM, gy = (g.N + BN - 1) / BN;
   NSG_CHECK(gx < (1ll << 31) && gy < 65536, NSG_ERR_UNSUPPORTED, "gemm: grid too large");
   // split K when the tile grid cannot fill the GPU
@@ -263,7 +337,7 @@ void gemm(nsg_ctx* c, const GemmArgs& g_in) {
     return;
   }
   if (c->precision == NSG_PREC_TF32X3 && gemm_split_tc(c, g)) return;
-  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g, 8)) return;
+  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g, 6)) return;
   gemm_f64_simt(c, g);
 }
 

@@ -127,7 +127,8 @@ __global__ void row_scale_kernel(const double* __restrict__ src, int64_t rows, i
       if (m > 0) {
         frexp(m, &e);  // m = f 2^e, f in [0.5, 1)  ->  m <= 2^e
       }
-      scale[t] = (m > 0) ? ldexp(1.0, e) : 1.0;
+      // a normal power of two (the slicer inverts it by exponent arithmetic)
+      scale[t] = (m > 0) ? ldexp(1.0, max(e, -1000)) : 1.0;
     }
   }
 }
@@ -158,13 +159,22 @@ __global__ void slice_kernel(const double* __restrict__ src, int64_t rows, int64
     __syncthreads();
     for (int i = ty; i < 32; i += 8) {
       int64_t r = rt * 32 + i, k = kt * 32 + tx;
-      double x = tile[i][tx] / scale[b * rows_p + r];  // |x| <= 1, exact (power of two)
+      // x = value / sigma_r in [-1, 1] (sigma_r a power of two: the product is exact),
+      // then X = round(x 2^{7S}) in int64 and balanced 7-bit digits of X peeled off from
+      // the top with integer shifts (round half up): X = sum_s d_s 2^{7(S-1-s)}, |d_0| <=
+      // 128, |d_s| <= 64 after it, and |x - X 2^{-7S}| <= 2^{-7S-1}.  Only one FP64
+      // multiply and one conversion per element: the FP64 pipe is the slow one here.
+      // 1 / sigma_r by exponent arithmetic (sigma_r is a normal power of two)
+      const double inv = __longlong_as_double(0x7FE0000000000000ll - __double_as_longlong(scale[b * rows_p + r]));
+      constexpr double kFix = double(1ull << (7 * S));
+      long long X = __double2ll_rn(tile[i][tx] * inv * kFix);
+#pragma unroll
       for (int s = 0; s < S; ++s) {
-        double y = x * 128.0;  // next 7 bits to the integer part (exact)
-        double dgt = rint(y);
-        x = y - dgt;           // remainder, |x| <= 1/2, exact
+        const int sh = 7 * (S - 1 - s);
+        const long long dgt = sh ? ((X + (1ll << (sh - 1))) >> sh) : X;
+        X -= dgt << sh;
         size_t o = ((size_t)(b * S + s) * rows_p + r) * K_p + k;
-        out[o] = __float2bfloat16_rn((float)dgt);  // |dgt| <= 128: exact in bf16
+        out[o] = __float2bfloat16_rn((float)(int)dgt);  // |dgt| <= 128: exact in bf16
       }
     }
     __syncthreads();
@@ -424,8 +434,7 @@ bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
   slice_operand<S>(c, (const double*)g.A, g.M, g.K, ars, aks, g.strideA, ab, Mp, Kp, sa, As);
   slice_operand<S>(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
   CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM, S), mB = make_map(Bs, Np, Kp, S * bb, BN, S);
-  int* err = (int*)dev_scratch(c, 1);
-  NSG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
+  int* err = device_flag(c);  // checked once at the end of the public call
   static bool attr = false;  // one flag per instantiation
   if (!attr) {
     NSG_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
@@ -441,10 +450,6 @@ bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
   count_launch(c);
   check_launch("oz_gemm");
   dfree(c, buf, bytes);
-  int herr = 0;
-  NSG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  NSG_CUDA(cudaStreamSynchronize(c->stream));
-  NSG_CHECK(herr == 0, NSG_ERR_TIMEOUT, "oz_gemm: a bounded mbarrier wait timed out");
   return true;
 }
 

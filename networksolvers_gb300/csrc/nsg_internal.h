@@ -60,6 +60,8 @@ struct nsg_ctx {
   // device scratch for reductions
   double* dev_scratch = nullptr;
   size_t dev_scratch_cap = 0;
+  int* dev_flag = nullptr;     // raised by tensor-core kernels whose bounded waits expired
+  bool flag_pending = false;   // a launch since the last check may have raised it
   int num_sms = 0;
   cudaEvent_t events[16] = {};
   bool profiling = false;
@@ -82,6 +84,11 @@ nsg_tensor* new_tensor(nsg_ctx* c, int dtype, int rank, const int64_t* dims, boo
 void free_tensor(nsg_ctx* c, nsg_tensor* t);
 double* host_scalars(nsg_ctx* c, size_t n);
 double* dev_scratch(nsg_ctx* c, size_t n);
+// The context's device error flag (zeroed on creation).  Kernels that may time out
+// write 1 into it instead of forcing a synchronisation per launch; every public entry
+// point checks it once at its end (check_device_flag) and reports NSG_ERR_TIMEOUT.
+int* device_flag(nsg_ctx* c);
+void check_device_flag(nsg_ctx* c);
 inline void count_launch(nsg_ctx* c, int n = 1) { c->launches += n; }
 
 // Brackets a kernel launch with CUDA events while the context is profiling.
@@ -164,6 +171,7 @@ void tridiag_eig(int n, const double* alpha, const double* beta, double* evals, 
 // extern "C" guard helper
 #define NSG_API_BEGIN(ctx) try {
 #define NSG_API_END(ctx)                                                   \
+  ::nsg::check_device_flag(ctx);                                           \
   }                                                                        \
   catch (const ::nsg::Error& e) {                                          \
     if (ctx) (ctx)->err = e.what();                                        \

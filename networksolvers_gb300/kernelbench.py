@@ -3,11 +3,18 @@
     python -m networksolvers_gb300.kernelbench factorize --n 1024 [--complex] [--precision fp64]
     python -m networksolvers_gb300.kernelbench heff --chi 512 [--precision ozaki]
     python -m networksolvers_gb300.kernelbench gemm --m 4096 --n 4096 --k 4096 [--precision ozaki]
+    python -m networksolvers_gb300.kernelbench region --chi 1024 --chi-right 512 [--precision ozaki]
 
 `factorize` is the inserter's truncated factorization (it.factorize, inserter.jl:23) of
 an n x n two-site matrix keeping n/2 states; `heff` one application of the two-site
 chain H_eff (optimal_map, operator_map.jl:3-10) at bond dimension chi with the
-Heisenberg MPO (w = 5, d = 2); `gemm` one plain product.  Each runs --warmup untimed
+Heisenberg MPO (w = 5, d = 2); `gemm` one plain product; `region` one full two-site
+DMRG region step (extracter with density-matrix expansion, Lanczos updater, inserter;
+iterators.jl:81-100) in the middle of a 24-site Heisenberg chain whose bonds are --chi
+left of the region and --chi-right from it on (the shape of a left-to-right sweep that
+raises the bond dimension from chi-right to chi), maxdim --chi.  For `region` the
+--warmup calls step the regions before the timed ones, so every timed call is the next
+region of the same sweep.  Each runs --warmup untimed
 and --reps timed calls and prints one JSON line with the mean time per call (CUDA
 events on the library's stream) and, with --profile, the per-class kernel times.
 These are small, self-contained cases meant for profiler captures of one kernel.
@@ -53,13 +60,50 @@ def _heff_case(chi, seed):
     return LinearMap(_FixedMap(fixed), inds), x
 
 
+def _region_case(chi, chi_right, precision, seed, ctx):
+    from . import models
+    from .network import euler_sweep
+    from .sweep import EigsolveProblem, RegionIterator, _prepare, region_iterator_action, updater_eigsolve
+    nsites = 24
+    g = models.chain_graph(nsites)
+    mid = nsites // 2
+    psi0 = models.random_state(g, 1, seed=seed)
+    rng = np.random.default_rng(seed)
+    dims = {}
+    for (u, v) in g.edges:
+        i = min(u, v)
+        cap = 2 ** min(i, nsites - i)
+        dims[(u, v)] = min(cap, chi if i < mid else chi_right)
+    for v in g.vertices:
+        shape = [2 if leg[0] == 's' else dims[leg[1]] for leg in psi0.legs[v]]
+        psi0.tensors[v] = rng.standard_normal(shape) / np.sqrt(np.prod(shape))
+    H = models.heisenberg_chain(nsites)
+    psi, P = _prepare(H, psi0, ctx)
+    prob = EigsolveProblem(psi, P)
+    trunc = dict(cutoff=1e-12, maxdim=chi)
+    plan = euler_sweep(psi.g, 2)
+    R = RegionIterator(prob, plan)
+    first = [k for k, (region, _) in enumerate(plan) if region[0] == mid][0]
+    kws = dict(extracter_kwargs=dict(trunc=trunc, subspace_algorithm="densitymatrix"),
+               updater_kwargs=dict(krylovdim=3, maxiter=1), inserter_kwargs=dict(trunc=trunc))
+    state = {"prob": prob, "k": first - 1}
+
+    def step():
+        state["k"] += 1
+        R.which = state["k"]
+        state["prob"] = region_iterator_action(state["prob"], R, updater_eigsolve, sweep=1, **kws)
+
+    return step
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m networksolvers_gb300.kernelbench")
-    ap.add_argument("op", choices=["factorize", "heff", "gemm"])
+    ap.add_argument("op", choices=["factorize", "heff", "gemm", "region"])
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--m", type=int, default=4096)
     ap.add_argument("--k", type=int, default=4096)
     ap.add_argument("--chi", type=int, default=512)
+    ap.add_argument("--chi-right", type=int, default=None)
     ap.add_argument("--complex", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=sorted(_native.PRECISIONS))
     ap.add_argument("--warmup", type=int, default=1)
@@ -86,6 +130,9 @@ def main(argv=None):
         run = lambda: lm(x)
         flops = lm.flops()
         case = {"chi": args.chi, "w": 5, "d": 2}
+    elif args.op == "region":
+        run = _region_case(args.chi, args.chi_right or args.chi // 2, args.precision, args.seed, ctx)
+        case = {"chi": args.chi, "chi_right": args.chi_right or args.chi // 2, "sites": 24}
     else:
         i, j, l = Index(args.m), Index(args.n), Index(args.k)
         A = DTensor.from_numpy(rng.standard_normal((args.m, args.k)), [i, l])
@@ -98,12 +145,15 @@ def main(argv=None):
     ctx.synchronize()
     if args.profile:
         ctx.profile(True)
+    launches0 = ctx.counters()["launches"]
     ctx.record(0)
     for _ in range(args.reps):
         run()
     ctx.record(1)
     ms = ctx.elapsed_ms(0, 1) / args.reps
-    line = {"op": args.op, "case": case, "precision": args.precision, "reps": args.reps, "ms_per_call": ms}
+    line = {"op": args.op, "case": case, "precision": args.precision, "reps": args.reps, "ms_per_call": ms,
+            "launches_before_timed": int(launches0),
+            "launches_per_call": (ctx.counters()["launches"] - launches0) / args.reps}
     if flops:
         line["tflops_fp64_equiv"] = flops / (ms / 1e3) / 1e12
     if args.profile:

@@ -59,6 +59,25 @@ def test_contract_layouts(nsg_ctx, cplx):
             assert rel(Cd.to_numpy(), ref) < 1e-12, (ia, ib, conj_a)
 
 
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("conj", [False, True])
+def test_site_operator_step(nsg_ctx, cplx, conj):
+    """The H_eff middle step: T[a', w1, s1, s2, b] . W[w1, s1, s2, x] over (w1, s1, s2),
+    a batched tall-skinny product (N, K <= 32) run by the one-row-per-thread kernel,
+    with and without conjugated operands."""
+    rng = np.random.default_rng(5)
+    a, w1, s1, s2, b, x = (Index(d) for d in (300, 5, 2, 2, 70, 20))
+    T = rnd(rng, (300, 5, 2, 2, 70), cplx)
+    W = rnd(rng, (5, 2, 2, 20), cplx)
+    At = DTensor.from_numpy(T, [a, w1, s1, s2, b])
+    Wt = DTensor.from_numpy(W, [w1, s1, s2, x])
+    if conj:
+        At, T = At.dag(), T.conj()
+    got = contract([At, Wt], out=[a, x, b]).to_numpy()
+    ref = np.einsum("awstb,wstx->axb", T, W)
+    assert rel(got, ref) < 1e-13
+
+
 def test_contract_network_and_output_order(nsg_ctx):
     rng = np.random.default_rng(2)
     chi, w, d = 9, 5, 2
