@@ -6,7 +6,8 @@
 //      origin at the nearer pole (one thread per root over many CTAs), Gu-Eisenstat
 //      recomputed z for orthogonal vectors, merged by an FP64 GEMM,
 //   3. back-transformation of the kept eigenvectors with the Householder reflectors
-//      in blocks of 128 (compact WY, three GEMMs per block).
+//      in blocks of 64 (compact WY, three GEMMs per block; every block's T factor is
+//      formed up front in one launch).
 // The merge GEMMs and the two large back-transformation GEMMs use the FP64-level
 // products (eight-slice Ozaki form in the split precision); the reflector Gram matrix
 // V^H V and T W stay on the FP64 cores (six-slice products there alone cost 1e-11 of
@@ -566,6 +567,214 @@ __global__ void merge_prep_kernel(const double* w, const double* Q, int n, const
   W.counts[3 * mi + 2] = flip;
 }
 
+// Shared-memory forms of the three serial steps of a merge (preparation with
+// deflation, compaction of the non-deflated slots, final ordering).  The CTA loads the
+// merge's data in parallel; the order-dependent loops then run in one thread on shared
+// memory (a few cycles per element instead of a global round trip), and the results are
+// written back in parallel.  Used for blocks of up to kSmemMerge rows.
+constexpr int kSmemMerge = 4096;  // 48 bytes of shared memory per row at most
+
+__global__ void merge_prep_smem_kernel(const double* w, const double* Q, int n, const MergeDesc* md, int nmerge,
+                                       MergeWork W) {
+  extern __shared__ double mp_smem[];
+  const int mi = blockIdx.x;
+  if (mi >= nmerge) return;
+  const MergeDesc M = md[mi];
+  const int lo = M.lo, mid = M.mid, hi = M.hi, nb = hi - lo, n1 = mid - lo;
+  double* ws = mp_smem;       // block eigenvalues
+  double* zr = ws + nb;       // z candidates by local index
+  double* Dsm = zr + nb;      // sorted D
+  double* zsm = Dsm + nb;     // sorted z
+  int* pm = (int*)(zsm + nb);  // sorted -> local index
+  int* kd = pm + nb;           // kind
+  __shared__ double red[32];
+  for (int li = threadIdx.x; li < nb; li += blockDim.x) {
+    ws[li] = w[lo + li];
+    zr[li] = (li < n1) ? Q[(size_t)(lo + li) * n + (mid - 1)] : Q[(size_t)(lo + li) * n + mid];
+  }
+  __syncthreads();
+  double rho = M.beta;
+  const int flip = rho < 0;
+  const double sg = flip ? -1.0 : 1.0;
+  if (flip) rho = -rho;
+  if (threadIdx.x == 0) {
+    int a = 0, b = 0;
+    for (int t = 0; t < nb; ++t) {
+      const int ia = flip ? (n1 - 1 - a) : a;
+      const int ib = flip ? (nb - 1 - b) : (n1 + b);
+      bool takeA;
+      if (a >= n1)
+        takeA = false;
+      else if (b >= nb - n1)
+        takeA = true;
+      else
+        takeA = sg * ws[ia] <= sg * ws[ib];
+      const int li = takeA ? ia : ib;
+      if (takeA)
+        ++a;
+      else
+        ++b;
+      pm[t] = li;
+      Dsm[t] = sg * ws[li];
+      zsm[t] = zr[li];
+    }
+  }
+  __syncthreads();
+  // |z| and max |D| (fixed-order block reductions)
+  double s2 = 0.0, dm = 0.0;
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    s2 += zsm[t] * zsm[t];
+    dm = fmax(dm, fabs(Dsm[t]));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+    dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
+  }
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ double redm[32];
+  if (lane == 0) {
+    red[warp] = s2;
+    redm[warp] = dm;
+  }
+  __syncthreads();
+  double nz = 0.0, dmax = 0.0;
+  for (int q = 0; q < nw; ++q) {
+    nz += red[q];
+    dmax = fmax(dmax, redm[q]);
+  }
+  nz = sqrt(nz);
+  rho = rho * nz * nz;
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) zsm[t] /= nz;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const double tol = 8.0 * 2.220446049250313e-16 * fmax(dmax, rho);
+    int k = 0, nrot = 0, prev = -1;
+    int* rpq = W.rot_pq + 2 * lo;
+    double* rcs = W.rot_cs + 2 * lo;
+    for (int t = 0; t < nb; ++t) {
+      if (rho * fabs(zsm[t]) <= tol) {
+        kd[t] = 0;
+        zsm[t] = 0.0;
+        continue;
+      }
+      kd[t] = 1;
+      if (prev >= 0 && fabs(Dsm[t] - Dsm[prev]) <= tol) {
+        const double r = hypot(zsm[t], zsm[prev]);
+        const double c = zsm[t] / r, sn = zsm[prev] / r;
+        const double dp = Dsm[prev], dt = Dsm[t];
+        Dsm[prev] = c * c * dp + sn * sn * dt;
+        Dsm[t] = sn * sn * dp + c * c * dt;
+        zsm[prev] = 0.0;
+        zsm[t] = r;
+        kd[prev] = 0;
+        rpq[2 * nrot] = pm[prev];
+        rpq[2 * nrot + 1] = pm[t];
+        rcs[2 * nrot] = c;
+        rcs[2 * nrot + 1] = sn;
+        ++nrot;
+      }
+      prev = t;
+    }
+    for (int t = 0; t < nb; ++t) k += kd[t];
+    W.rho[mi] = rho;
+    W.counts[3 * mi] = k;
+    W.counts[3 * mi + 1] = nrot;
+    W.counts[3 * mi + 2] = flip;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    W.Ds[lo + t] = Dsm[t];
+    W.zs[lo + t] = zsm[t];
+    W.perm[lo + t] = pm[t];
+    W.kind[lo + t] = kd[t];
+  }
+}
+
+__global__ void gather_nondeflated_smem_kernel(int nb, const int* kind, const double* Ds, const double* zs, int* kpos,
+                                               double* Dk, double* zk) {
+  extern __shared__ int gn_smem[];
+  int* kd = gn_smem;
+  int* kp = kd + nb;
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) kd[t] = kind[t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int k = 0;
+    for (int t = 0; t < nb; ++t) {
+      kp[t] = kd[t] ? k : -1;
+      k += kd[t];
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    const int q = kp[t];
+    kpos[t] = q;
+    if (q >= 0) {
+      Dk[q] = Ds[t];
+      zk[q] = zs[t];
+    }
+  }
+}
+
+__global__ void merge_finalize_order_smem_kernel(const double* Ds, const int* kind, const double* lam, int nb, int flip,
+                                                 int* src_kind, int* src_idx, double* wout) {
+  extern __shared__ double mf_smem[];
+  double* Dsm = mf_smem;
+  double* lm = Dsm + nb;
+  double* wo = lm + nb;
+  int* kd = (int*)(wo + nb);
+  int* sk = kd + nb;
+  int* si = sk + nb;
+  __shared__ int s_nr;
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    Dsm[t] = Ds[t];
+    kd[t] = kind[t];
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nr = 0;
+    for (int t = 0; t < nb; ++t) nr += kd[t];
+    s_nr = nr;
+  }
+  __syncthreads();
+  const int nr = s_nr, nd = nb - nr;
+  for (int t = threadIdx.x; t < nr; t += blockDim.x) lm[t] = lam[t];
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ia = 0, ib = 0, pos = 0, dslot = 0;
+    while (dslot < nb && kd[dslot]) ++dslot;
+    while (ia < nr || ib < nd) {
+      bool takeRoot;
+      if (ia >= nr)
+        takeRoot = false;
+      else if (ib >= nd)
+        takeRoot = true;
+      else
+        takeRoot = lm[ia] <= Dsm[dslot];
+      const int out = flip ? (nb - 1 - pos) : pos;
+      if (takeRoot) {
+        sk[out] = 1;
+        si[out] = ia;
+        wo[out] = flip ? -lm[ia] : lm[ia];
+        ++ia;
+      } else {
+        sk[out] = 0;
+        si[out] = dslot;
+        wo[out] = flip ? -Dsm[dslot] : Dsm[dslot];
+        ++ib;
+        ++dslot;
+        while (dslot < nb && kd[dslot]) ++dslot;
+      }
+      ++pos;
+    }
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    src_kind[t] = sk[t];
+    src_idx[t] = si[t];
+    wout[t] = wo[t];
+  }
+}
+
 // Apply the deflation rotations to the block's columns: one thread per row.
 __global__ void merge_rot_kernel(double* Q, int n, const MergeDesc* md, int mi, MergeWork W, int nrot) {
   const MergeDesc M = md[mi];
@@ -836,43 +1045,51 @@ __global__ void scale_rows_phase_kernel(double2* Z, int64_t rows, int64_t cols, 
   }
 }
 
-// compact WY: T factor (upper triangular, nbk x nbk <= 128) for reflectors
-// k0..k0+nbk-1 from S = V^H V: T_jj = tau_j, T[0:j, j] = -tau_j T[0:j,0:j] S[0:j, j];
-// one CTA, thread i owns row i.
+// compact WY: T factors of all reflector blocks in one launch (block b = CTA b; kWY = 64
+// reflectors per block, zero-padded with tau = 0) from S_b = V_b^H V_b:
+// T_jj = tau_j, T[0:j, j] = -tau_j T[0:j, 0:j] S[0:j, j]; thread i owns row i; S_b and T_b
+// live in shared memory.
+constexpr int kWY = 64;
 template <typename T>
-__global__ void wy_tfactor_kernel(const T* S, int nbk, const T* tau, T* Tm) {
-  const int i = threadIdx.x;
-  if (blockIdx.x != 0) return;
-  for (int j = 0; j < nbk; ++j)
-    if (i < nbk) Tm[i + j * nbk] = czero<T>();
+__global__ void __launch_bounds__(kWY) wy_tfactor_kernel(const T* S, const T* tau, T* Tm) {
+  extern __shared__ unsigned char wy_smem[];  // 2 x kWY x (kWY + 1) elements
+  T(*Ss)[kWY + 1] = (T(*)[kWY + 1])wy_smem;
+  T(*Ts)[kWY + 1] = Ss + kWY;
+  const int i = threadIdx.x, b = blockIdx.x;
+  const T* Sb = S + (size_t)b * kWY * kWY;
+  const T* tb = tau + (size_t)b * kWY;
+  T* Tb = Tm + (size_t)b * kWY * kWY;
+  for (int j = 0; j < kWY; ++j) {
+    Ss[i][j] = Sb[i + j * kWY];
+    Ts[i][j] = czero<T>();
+  }
   __syncthreads();
-  for (int j = 0; j < nbk; ++j) {
+  for (int j = 0; j < kWY; ++j) {
     T acc = czero<T>();
     if (i < j)
-      for (int l = i; l < j; ++l) acc = cadd(acc, cmulv(Tm[i + l * nbk], S[l + j * nbk]));
-    __syncthreads();
-    if (i < j) Tm[i + j * nbk] = cscale(cmulv(tau[j], acc), -1.0);
-    if (i == j) Tm[j + j * nbk] = tau[j];
+      for (int l = i; l < j; ++l) acc = cadd(acc, cmulv(Ts[i][l], Ss[l][j]));
+    if (i < j) Ts[i][j] = cscale(cmulv(tb[j], acc), -1.0);  // column j: read only columns < j above
+    if (i == j) Ts[j][j] = tb[j];
     __syncthreads();
   }
+  for (int j = 0; j < kWY; ++j) Tb[i + j * kWY] = Ts[i][j];
 }
 
-// Extract reflector block V (rows k0+1..n-1, unit diagonal, zeros above) from A.
+// all reflectors as the columns of an n x ncols matrix (v_kk[kk+1] = 1, zeros above,
+// zero columns beyond the last reflector)
 template <typename T>
-__global__ void wy_extract_kernel(const T* A, int n, int k0, int nbk, T* V) {
-  int rows = n - (k0 + 1);
-  size_t tot = (size_t)rows * nbk;
+__global__ void wy_extract_all_kernel(const T* A, int n, int nref, int ncols, T* V) {
+  const size_t tot = (size_t)n * ncols;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    int r = int(e % rows), j = int(e / rows);
-    int gr = k0 + 1 + r, kk = k0 + j;  // reflector kk has v[kk+1] = 1, support rows > kk
-    T val;
-    if (gr < kk + 1)
-      val = czero<T>();
-    else if (gr == kk + 1)
-      val = cone<T>();
-    else
-      val = A[gr + (size_t)kk * n];
-    V[r + (size_t)j * rows] = val;
+    const int r = int(e % n), kk = int(e / n);
+    T val = czero<T>();
+    if (kk < nref) {
+      if (r == kk + 1)
+        val = cone<T>();
+      else if (r > kk + 1)
+        val = A[r + (size_t)kk * n];
+    }
+    V[e] = val;
   }
 }
 
@@ -960,7 +1177,15 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
     W.rho = brho.as<double>();
     W.counts = bcnt.as<int>();
     NSG_CUDA(cudaMemcpyAsync(bmd.p, lv.data(), sizeof(MergeDesc) * nm, cudaMemcpyHostToDevice, c->stream));
-    merge_prep_kernel<<<nm, 32, 0, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
+    int maxnb = 0;
+    for (auto& m : lv) maxnb = std::max(maxnb, m.hi - m.lo);
+    if (maxnb <= kSmemMerge) {
+      const int shm = maxnb * (6 * 8);
+      NSG_CUDA(cudaFuncSetAttribute(merge_prep_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      merge_prep_smem_kernel<<<nm, 256, shm, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
+    } else {
+      merge_prep_kernel<<<nm, 32, 0, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
+    }
     count_launch(c);
     check_launch("dc prep");
     std::vector<double> rho(nm);
@@ -978,9 +1203,17 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       DevBuf Dk(c, sizeof(double) * std::max(k, 1)), zk(c, sizeof(double) * std::max(k, 1)),
           kpos(c, sizeof(int) * nb), lam(c, sizeof(double) * std::max(k, 1));
       DevBuf Qk(c, sizeof(double) * (size_t)nb * std::max(k, 1)), Qm(c, sizeof(double) * (size_t)nb * std::max(k, 1));
-      gather_nondeflated_kernel<<<1, 32, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, W.kind + M.lo, W.Ds + M.lo,
-                                                         W.zs + M.lo, kpos.as<int>(), Qk.as<double>(), Dk.as<double>(),
-                                                         zk.as<double>());
+      if (nb <= kSmemMerge) {
+        const int shm = nb * 8;
+        NSG_CUDA(cudaFuncSetAttribute(gather_nondeflated_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      shm));
+        gather_nondeflated_smem_kernel<<<1, 256, shm, c->stream>>>(nb, W.kind + M.lo, W.Ds + M.lo, W.zs + M.lo,
+                                                                   kpos.as<int>(), Dk.as<double>(), zk.as<double>());
+      } else {
+        gather_nondeflated_kernel<<<1, 32, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, W.kind + M.lo,
+                                                           W.Ds + M.lo, W.zs + M.lo, kpos.as<int>(), Qk.as<double>(),
+                                                           Dk.as<double>(), zk.as<double>());
+      }
       int gblocks = int(std::min<size_t>(((size_t)nb * nb + 255) / 256, (size_t)c->num_sms * 8));
       gather_cols_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, kpos.as<int>(),
                                                          Qk.as<double>());
@@ -1015,8 +1248,17 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       }
       DevBuf skind(c, sizeof(int) * nb), sidx(c, sizeof(int) * nb), wnew(c, sizeof(double) * nb),
           Qnew(c, sizeof(double) * (size_t)nb * nb);
-      merge_finalize_order_kernel<<<1, 32, 0, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(), nb, flip,
-                                                           skind.as<int>(), sidx.as<int>(), wnew.as<double>());
+      if (nb <= kSmemMerge) {
+        const int shm = nb * (3 * 8 + 3 * 4);
+        NSG_CUDA(cudaFuncSetAttribute(merge_finalize_order_smem_kernel,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        merge_finalize_order_smem_kernel<<<1, 256, shm, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(),
+                                                                     nb, flip, skind.as<int>(), sidx.as<int>(),
+                                                                     wnew.as<double>());
+      } else {
+        merge_finalize_order_kernel<<<1, 32, 0, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(), nb, flip,
+                                                             skind.as<int>(), sidx.as<int>(), wnew.as<double>());
+      }
       merge_scatter_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, Qm.as<double>(),
                                                            skind.as<int>(), sidx.as<int>(), Qnew.as<double>());
       copy_block_kernel<<<gblocks, 256, 0, c->stream>>>(Qnew.as<double>(), nb, Q, n, M.lo, wnew.as<double>(), w);
@@ -1028,45 +1270,60 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
 
 template <typename T>
 static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* tau_dev, T* Z, int64_t ldz, int64_t k) {
-  // Z <- H_0 H_1 ... H_{n-3} Z, blocks of 128 reflectors applied last block first
+  // Z <- H_0 H_1 ... H_{n-3} Z in blocks of kWY reflectors, last block first.  Every
+  // block's V, S = V^H V and T factor are formed up front (one launch each); the
+  // sequential part is then three GEMMs per block.
   const int nref = n - 2;
   if (nref <= 0 || k == 0) return;
-  const int NB = 128;
+  const int NB = kWY, nblk = (nref + NB - 1) / NB, ncols = nblk * NB;
   const size_t eb = sizeof(T);
-  DevBuf V(c, eb * (size_t)n * NB), S(c, eb * NB * NB), Tm(c, eb * NB * NB), Wt(c, eb * (size_t)NB * k),
-      W2(c, eb * (size_t)NB * k);
-  for (int k0 = ((nref - 1) / NB) * NB; k0 >= 0; k0 -= NB) {
-    int nbk = std::min(NB, nref - k0);
-    int rows = n - (k0 + 1);
-    int gblocks = int(std::min<size_t>(((size_t)rows * nbk + 255) / 256, (size_t)c->num_sms * 8));
-    wy_extract_kernel<T><<<gblocks, 256, 0, c->stream>>>(A, n, k0, nbk, V.as<T>());
+  DevBuf V(c, eb * (size_t)n * ncols), S(c, eb * (size_t)NB * NB * nblk), Tm(c, eb * (size_t)NB * NB * nblk),
+      taup(c, eb * ncols), Wt(c, eb * (size_t)NB * k), W2(c, eb * (size_t)NB * k);
+  {
+    int gblocks = int(std::min<size_t>(((size_t)n * ncols + 255) / 256, (size_t)c->num_sms * 8));
+    wy_extract_all_kernel<T><<<gblocks, 256, 0, c->stream>>>(A, n, nref, ncols, V.as<T>());
+    NSG_CUDA(cudaMemsetAsync(taup.p, 0, eb * ncols, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(taup.p, tau_dev, eb * nref, cudaMemcpyDeviceToDevice, c->stream));
     count_launch(c);
-    // S = V^H V
-    GemmArgs g;
-    g.dtype = dtype;
-    g.batch = 1;
-    g.strideA = g.strideB = g.strideC = 0;
-    g.M = nbk;
-    g.N = nbk;
-    g.K = rows;
-    g.A = V.p;
-    g.lda = rows;
-    g.opA = OP_C;
-    g.B = V.p;
-    g.ldb = rows;
-    g.opB = OP_N;
-    g.C = S.p;
-    g.ldc = nbk;
-    gemm_f64_simt(c, g);
-    wy_tfactor_kernel<T><<<1, 128, 0, c->stream>>>(S.as<T>(), nbk, tau_dev + k0, Tm.as<T>());
-    count_launch(c);
-    // W = V^H Z(rows k0+1..)  (nbk x k)
-    GemmArgs h = g;
+  }
+  // S_b = V_b^H V_b over all n rows (rows above a block's reflectors are zero)
+  GemmArgs g;
+  g.dtype = dtype;
+  g.M = NB;
+  g.N = NB;
+  g.K = n;
+  g.A = V.p;
+  g.lda = n;
+  g.opA = OP_C;
+  g.strideA = (int64_t)n * NB;
+  g.B = V.p;
+  g.ldb = n;
+  g.opB = OP_N;
+  g.strideB = (int64_t)n * NB;
+  g.C = S.p;
+  g.ldc = NB;
+  g.strideC = (int64_t)NB * NB;
+  g.batch = nblk;
+  gemm_f64_simt(c, g);
+  {
+    const int shm = int(2 * NB * (NB + 1) * eb);
+    NSG_CUDA(cudaFuncSetAttribute(wy_tfactor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+    wy_tfactor_kernel<T><<<nblk, NB, shm, c->stream>>>(S.as<T>(), taup.as<T>(), Tm.as<T>());
+  }
+  count_launch(c);
+  for (int b = nblk - 1; b >= 0; --b) {
+    const int k0 = b * NB, nbk = std::min(NB, nref - k0), rows = n - (k0 + 1);
+    const T* Vb = V.as<T>() + (k0 + 1) + (size_t)k0 * n;
+    // W = V_b^H Z(rows k0+1..)  (nbk x k)
+    GemmArgs h;
+    h.dtype = dtype;
+    h.batch = 1;
+    h.strideA = h.strideB = h.strideC = 0;
     h.M = nbk;
     h.N = k;
     h.K = rows;
-    h.A = V.p;
-    h.lda = rows;
+    h.A = Vb;
+    h.lda = n;
     h.opA = OP_C;
     h.B = Z + (k0 + 1);
     h.ldb = ldz;
@@ -1074,13 +1331,13 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
     h.C = Wt.p;
     h.ldc = nbk;
     gemm_accurate(c, h);
-    // W2 = T W
-    GemmArgs t2 = g;
+    // W2 = T_b W
+    GemmArgs t2 = h;
     t2.M = nbk;
     t2.N = k;
     t2.K = nbk;
-    t2.A = Tm.p;
-    t2.lda = nbk;
+    t2.A = Tm.as<T>() + (size_t)b * NB * NB;
+    t2.lda = NB;
     t2.opA = OP_N;
     t2.B = Wt.p;
     t2.ldb = nbk;
@@ -1088,13 +1345,13 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
     t2.C = W2.p;
     t2.ldc = nbk;
     gemm_f64_simt(c, t2);
-    // Z -= V W2
-    GemmArgs u = g;
+    // Z -= V_b W2
+    GemmArgs u = h;
     u.M = rows;
     u.N = k;
     u.K = nbk;
-    u.A = V.p;
-    u.lda = rows;
+    u.A = Vb;
+    u.lda = n;
     u.opA = OP_N;
     u.B = W2.p;
     u.ldb = nbk;
