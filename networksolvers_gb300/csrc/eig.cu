@@ -266,6 +266,38 @@ nsg_tensor* matricize(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int
   return P;
 }
 
+
+// Y[:, j] *= f[j]  (column scaling)
+template <typename T>
+__global__ void col_scale_kernel(T* Y, int64_t rows, int64_t cols, const double* f) {
+  const int64_t tot = rows * cols;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+    const double s = f[e / rows];
+    if constexpr (sizeof(T) == 8) {
+      Y[e] *= s;
+    } else {
+      Y[e].x *= s;
+      Y[e].y *= s;
+    }
+  }
+}
+
+// G <- 1.5 I - 0.5 G (k x k): the first-order inverse square root of a Gram matrix
+// that is the identity up to small terms (symmetric re-orthogonalisation)
+template <typename T>
+__global__ void half_newton_kernel(T* G, int64_t k) {
+  const int64_t tot = k * k;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+    const bool diag = (e % k) == (e / k);
+    if constexpr (sizeof(T) == 8) {
+      G[e] = (diag ? 1.5 : 0.0) - 0.5 * G[e];
+    } else {
+      G[e].x = (diag ? 1.5 : 0.0) - 0.5 * G[e].x;
+      G[e].y = -0.5 * G[e].y;
+    }
+  }
+}
+
 }  // namespace
 
 void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* w) {
@@ -291,6 +323,182 @@ void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev) {
 }  // namespace nsg
 
 using namespace nsg;
+
+namespace {
+struct DevBuf1 {
+  nsg_ctx* c;
+  void* p;
+  size_t bytes;
+  DevBuf1(nsg_ctx* cc, size_t b) : c(cc), p(dalloc(cc, b)), bytes(b) {}
+  ~DevBuf1() { dfree(c, p, bytes); }
+};
+}  // namespace
+
+// Tall M (m > ncol): truncated factorisation from the smaller Gram matrix M^H M
+// = V S^2 V^H.  U = M V_k S_k^{-1} carries a relative column error ~ eps s_max / s_k,
+// removed by symmetric re-orthogonalisation U <- U (3 I - U^H U) / 2 (each step squares
+// it; two steps when eps s_max / s_k > 1e-8); C = U^H M as in the square route.  The
+// spectrum and the truncation rule are those of M M^H (same non-zero eigenvalues).
+// Returns false, having allocated nothing that outlives it, when s_k^2 <= 1e-11 s_max^2
+// (s_k not resolved by the Gram matrix well above its rounding): the caller then takes
+// the M M^H route.
+static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, const std::vector<int64_t>& ldims,
+                            const std::vector<int64_t>& rdims, double sc, double cutoff, int64_t maxdim,
+                            int64_t mindim, nsg_tensor** Uo, nsg_tensor** Co, int64_t* ko, double* erro,
+                            std::vector<double>& P) {
+  const int dt = M->dtype;
+  const size_t eb = elem_bytes(dt);
+  const int64_t n = ncol;
+  void* G = dalloc(c, eb * n * n);
+  GemmArgs g;
+  g.dtype = dt;
+  g.M = n;
+  g.N = n;
+  g.K = m;
+  g.A = M->data;
+  g.lda = m;
+  g.opA = OP_C;
+  g.B = M->data;
+  g.ldb = m;
+  g.opB = OP_N;
+  g.C = G;
+  g.ldc = n;
+  g.batch = 1;
+  g.strideA = g.strideB = g.strideC = 0;
+  gemm_f64_simt(c, g);  // FP64 in every precision mode: the Gram matrix fixes the truncation
+  int64_t k = 0;
+  double err = 0.0, delta = 0.0;
+  bool ok = true;
+  void* V = nullptr;
+  size_t vbytes = 0;
+  std::vector<double> w;
+  PickFn pick = [&](const std::vector<double>& wa, void** Z, int64_t* ldz) {
+    P.assign(wa.rbegin(), wa.rend());
+    k = truncate_rule(P, n, cutoff, maxdim, mindim, &err);
+    // the Gram eigenvalues carry ~1e-15 P[0] of rounding: s_k must be resolved well above it
+    const double smax = std::sqrt(std::max(P[0], 0.0)), smin = std::sqrt(std::max(P[k - 1], 0.0));
+    ok = smax > 0.0 && P[k - 1] > 1e-11 * P[0];
+    if (!ok) return std::vector<int>();
+    delta = 1e-16 * smax / smin;
+    vbytes = eb * size_t(n) * size_t(k);
+    V = dalloc(c, vbytes);
+    *Z = V;
+    *ldz = n;
+    std::vector<int> cols(k);
+    for (int64_t i = 0; i < k; ++i) cols[i] = int(n - 1 - i);
+    return cols;
+  };
+  try {
+    syevd_dc(c, dt, int(n), G, w, pick);
+  } catch (...) {
+    dfree(c, G, eb * n * n);
+    if (V) dfree(c, V, vbytes);
+    throw;
+  }
+  dfree(c, G, eb * n * n);
+  if (!ok) return false;
+  // Y = M V_k S_k^{-1}
+  std::vector<int64_t> udims = ldims;
+  udims.push_back(k);
+  nsg_tensor* Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+  GemmArgs y;
+  y.dtype = dt;
+  y.M = m;
+  y.N = k;
+  y.K = n;
+  y.A = M->data;
+  y.lda = m;
+  y.opA = OP_N;
+  y.B = V;
+  y.ldb = n;
+  y.opB = OP_N;
+  y.C = Ut->data;
+  y.ldc = m;
+  y.batch = 1;
+  y.strideA = y.strideB = y.strideC = 0;
+  gemm_accurate(c, y);
+  dfree(c, V, vbytes);
+  {
+    std::vector<double> inv(k);
+    for (int64_t i = 0; i < k; ++i) inv[i] = 1.0 / std::sqrt(P[i]);
+    DevBuf1 f(c, sizeof(double) * k);
+    NSG_CUDA(cudaMemcpyAsync(f.p, inv.data(), sizeof(double) * k, cudaMemcpyHostToDevice, c->stream));
+    const int gb = int(std::min<int64_t>((m * k + 255) / 256, int64_t(c->num_sms) * 8));
+    if (dt == NSG_C128)
+      col_scale_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Ut->data, m, k, (const double*)f.p);
+    else
+      col_scale_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Ut->data, m, k, (const double*)f.p);
+    count_launch(c);
+    NSG_CUDA(cudaStreamSynchronize(c->stream));  // inv leaves scope
+  }
+  // symmetric re-orthogonalisation
+  const int iters = delta > 1e-8 ? 2 : 1;
+  nsg_tensor* Y2 = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+  void* Gk = dalloc(c, eb * k * k);
+  for (int it = 0; it < iters; ++it) {
+    GemmArgs q = y;
+    q.M = k;
+    q.N = k;
+    q.K = m;
+    q.A = Ut->data;
+    q.lda = m;
+    q.opA = OP_C;
+    q.B = Ut->data;
+    q.ldb = m;
+    q.opB = OP_N;
+    q.C = Gk;
+    q.ldc = k;
+    gemm_accurate(c, q);
+    const int gb = int(std::min<int64_t>((k * k + 255) / 256, int64_t(c->num_sms) * 8));
+    if (dt == NSG_C128)
+      half_newton_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Gk, k);
+    else
+      half_newton_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Gk, k);
+    count_launch(c);
+    GemmArgs r = y;
+    r.M = m;
+    r.N = k;
+    r.K = k;
+    r.A = Ut->data;
+    r.lda = m;
+    r.opA = OP_N;
+    r.B = Gk;
+    r.ldb = k;
+    r.opB = OP_N;
+    r.C = Y2->data;
+    r.ldc = m;
+    gemm_accurate(c, r);
+    std::swap(Ut, Y2);
+  }
+  dfree(c, Gk, eb * k * k);
+  free_tensor(c, Y2);
+  check_launch("factorize (tall)");
+  // C = U^H M
+  std::vector<int64_t> cdims;
+  cdims.push_back(k);
+  for (auto d : rdims) cdims.push_back(d);
+  nsg_tensor* Ct = new_tensor(c, dt, int(cdims.size()), cdims.data(), false);
+  GemmArgs h = y;
+  h.M = k;
+  h.N = ncol;
+  h.K = m;
+  h.A = Ut->data;
+  h.lda = m;
+  h.opA = OP_C;
+  h.B = M->data;
+  h.ldb = m;
+  h.opB = OP_N;
+  h.C = Ct->data;
+  h.ldc = k;
+  h.alpha_re = sc;
+  gemm_accurate(c, h);
+  *Uo = Ut;
+  *Co = Ct;
+  *ko = k;
+  *erro = err;
+  return true;
+}
+
 
 static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, double cutoff,
                           int64_t maxdim, int64_t mindim, nsg_tensor** U, nsg_tensor** C, int64_t* newdim,
@@ -319,6 +527,31 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
       owned = true;
     }
     scale(c, dt, M->size, 1.0 / sc, 0.0, M->data);
+  }
+  if (ncol < m && ncol >= 16) {
+    std::vector<double> Pr;
+    nsg_tensor *Ur = nullptr, *Cr = nullptr;
+    int64_t kr = 0;
+    double er = 0.0;
+    bool done;
+    try {
+      done = factorize_right(c, M, m, ncol, ldims, rdims, sc, cutoff, maxdim, mindim, &Ur, &Cr, &kr, &er, Pr);
+    } catch (...) {
+      if (owned) free_tensor(c, M);
+      throw;
+    }
+    if (done) {
+      if (owned) free_tensor(c, M);
+      if (spectrum)
+        for (int64_t i = 0; i < std::min<int64_t>(spectrum_cap, ncol); ++i)
+          spectrum[i] = i < int64_t(Pr.size()) ? std::max(Pr[i], 0.0) * sc * sc : 0.0;
+      *U = Ur;
+      *C = Cr;
+      if (newdim) *newdim = kr;
+      if (truncerr) *truncerr = er;
+      check_device_flag(c);
+      return NSG_OK;
+    }
   }
   // G = M M^H (FP64 in every precision mode: the Gram matrix fixes the truncation)
   void* G = dalloc(c, eb * m * m);

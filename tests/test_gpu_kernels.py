@@ -117,8 +117,11 @@ def _spectrum_matrix(rng, m, n, decay, cplx):
 
 
 @pytest.mark.parametrize("cplx", [False, True])
-@pytest.mark.parametrize("m,n", [(16, 16), (24, 10), (10, 24), (128, 128)])
+@pytest.mark.parametrize("m,n", [(16, 16), (24, 10), (10, 24), (128, 128), (200, 24), (300, 20)])
 def test_factorize_truncation(nsg_ctx, cplx, m, n):
+    """Singular values 0.55^i.  The tall shapes take the tall route (Gram matrix of the
+    narrow side, re-orthogonalised U) whenever the kept spectrum is resolved well above
+    the Gram matrix's rounding, the M M^H route otherwise."""
     rng = np.random.default_rng(m * 100 + n)
     M = _spectrum_matrix(rng, m, n, 0.55, cplx)
     l, r = Index(m), Index(n)
