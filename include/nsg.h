@@ -58,7 +58,9 @@ extern "C" {
 #define NSG_PREC_TF32X3 1        /* large contractions: 3 TF32 products, FP32 accumulate  */
 #define NSG_PREC_OZAKI 2         /* large contractions: 6 BF16 slices per operand, 21
                                     products, exact FP32 accumulation per 128-deep chunk:
-                                    FP64-level accuracy on the tensor cores              */
+                                    1e-12-level accuracy on the tensor cores             */
+#define NSG_PREC_OZAKI8 3        /* as NSG_PREC_OZAKI with 8 slices (36 products): FP64
+                                    accuracy (2^-55 of the row and column scales)        */
 
 #define NSG_MAX_RANK 16
 

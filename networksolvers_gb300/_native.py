@@ -14,7 +14,8 @@ _LIB = None
 OK, ERR_INVALID, ERR_OOM, ERR_CUDA, ERR_NONFINITE, ERR_NOT_CONVERGED, ERR_TIMEOUT, ERR_UNSUPPORTED = range(8)
 F64, C128 = 0, 1
 PREC_FP64, PREC_TF32X3, PREC_OZAKI = 0, 1, 2
-PRECISIONS = {"fp64": PREC_FP64, "tf32x3": PREC_TF32X3, "ozaki": PREC_OZAKI}
+PREC_OZAKI8 = 3
+PRECISIONS = {"fp64": PREC_FP64, "tf32x3": PREC_TF32X3, "ozaki": PREC_OZAKI, "ozaki8": PREC_OZAKI8}
 
 
 class NsgError(RuntimeError):

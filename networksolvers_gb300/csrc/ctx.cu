@@ -164,7 +164,7 @@ const char* nsg_last_error(const nsg_ctx* c) { return c ? c->err.c_str() : "null
 
 int nsg_ctx_set_precision(nsg_ctx* c, int precision) {
   NSG_API_BEGIN(c)
-  NSG_CHECK(precision >= NSG_PREC_FP64 && precision <= NSG_PREC_OZAKI, NSG_ERR_INVALID,
+  NSG_CHECK(precision >= NSG_PREC_FP64 && precision <= NSG_PREC_OZAKI8, NSG_ERR_INVALID,
             "unknown precision mode");
   c->precision = precision;
   NSG_API_END(c)

@@ -318,7 +318,7 @@ void gemm_accurate(nsg_ctx* c, const GemmArgs& g_in) {
     if (g.opB == OP_C) g.opB = OP_T;
     if (g.opB == OP_R) g.opB = OP_N;
   }
-  if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g, 8)) return;
+  if ((c->precision == NSG_PREC_OZAKI || c->precision == NSG_PREC_OZAKI8) && gemm_ozaki_tc(c, g, 8)) return;
   gemm_f64_simt(c, g);
 }
 
@@ -338,6 +338,7 @@ void gemm(nsg_ctx* c, const GemmArgs& g_in) {
   }
   if (c->precision == NSG_PREC_TF32X3 && gemm_split_tc(c, g)) return;
   if (c->precision == NSG_PREC_OZAKI && gemm_ozaki_tc(c, g, 6)) return;
+  if (c->precision == NSG_PREC_OZAKI8 && gemm_ozaki_tc(c, g, 8)) return;
   gemm_f64_simt(c, g);
 }
 

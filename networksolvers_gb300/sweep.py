@@ -170,10 +170,11 @@ def subspace_expand(problem, local, region_iterator, algorithm, trunc, expansion
         return problem, local
     tr = dict(trunc, maxdim=expand)
     # the expansion's projections are checked against a 1e-10 orthogonality guard
-    # (densitymatrix.jl:59): its contractions run in FP64 whatever the context's mode
+    # (densitymatrix.jl:59): its contractions run at FP64 accuracy whatever the context's
+    # mode (eight-slice tensor-core products in the split form, FP64 cores otherwise)
     ctx = A.ctx
     prec = ctx.precision
-    ctx.set_precision("fp64")
+    ctx.set_precision("ozaki8" if prec in ("ozaki", "ozaki8") else "fp64")
     try:
         return _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass)
     finally:

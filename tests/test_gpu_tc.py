@@ -75,3 +75,25 @@ def test_ozaki_gemm_fp64_level(nsg_ctx, m, k, n):
         # the method's bound is relative to the row/column scales (one wide row here)
         assert np.max(np.abs(c - ref) / scale) < 1e-13, (ia, ib)
         assert rel(c, ref) < 5e-11
+
+
+@pytest.mark.parametrize("m,k,n", [(200, 100, 300), (1024, 1024, 1024), (130, 4000, 70)])
+def test_ozaki8_gemm_fp64_accuracy(nsg_ctx, m, k, n):
+    """Eight slices (36 products): slicing error 2^-57 of the row and column scales per
+    product; the double-float (2 x FP32) chunk accumulation sets the floor near 1e-15 of
+    the scales, with one wide-range column as in the environments."""
+    rng = np.random.default_rng(m + 5 * k + n)
+    i, j, l = Index(m), Index(n), Index(k)
+    a = rng.standard_normal((m, k))
+    a[:, 0] *= 1e4
+    b = rng.standard_normal((k, n))
+    ref = a @ b
+    A, B = DTensor.from_numpy(a, (i, l)), DTensor.from_numpy(b, (l, j))
+    nsg_ctx.set_precision("ozaki8")
+    try:
+        c = contract([A, B], out=[i, j]).to_numpy()
+    finally:
+        nsg_ctx.set_precision("fp64")
+    scale = np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :] * k
+    assert np.max(np.abs(c - ref) / scale) < 1e-15
+    assert rel(c, ref) < 1e-13
