@@ -78,6 +78,9 @@ int nsg_ctx_set_precision(nsg_ctx* ctx, int precision);
 int nsg_ctx_synchronize(nsg_ctx* ctx);
 /* bytes in use / peak / budget */
 int nsg_ctx_memory(const nsg_ctx* ctx, uint64_t* in_use, uint64_t* peak, uint64_t* budget);
+/* Free and total device memory of `device` (cudaMemGetInfo): the admission budget of a
+   pool of concurrent solves.  No counterpart in the reference (single solve per process). */
+int nsg_device_memory(int device, uint64_t* free_bytes, uint64_t* total_bytes);
 /* counters[0] = kernel launches, [1] = algorithmic flops of contractions,
  * [2] = contraction calls, [3] = linear-map applications; reset if `reset`. */
 int nsg_ctx_counters(nsg_ctx* ctx, uint64_t* counters4, int reset);

@@ -6,6 +6,7 @@ usable, `lib()` raises.
 from __future__ import annotations
 
 import ctypes as C
+import threading
 import os
 from pathlib import Path
 
@@ -42,6 +43,7 @@ _SIGS = {
     "nsg_ctx_set_precision": (i32, [p, i32]),
     "nsg_ctx_synchronize": (i32, [p]),
     "nsg_ctx_memory": (i32, [p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
+    "nsg_device_memory": (i32, [i32, C.POINTER(u64), C.POINTER(u64)]),
     "nsg_ctx_counters": (i32, [p, C.POINTER(u64), i32]),
     "nsg_ctx_event_record": (i32, [p, i32]),
     "nsg_ctx_event_elapsed": (i32, [p, i32, i32, C.POINTER(C.c_float)]),
@@ -169,15 +171,37 @@ class Context:
 
 
 _default = None
+_local = threading.local()
 
 
 def default_context():
+    """The calling thread's context if it set one (worker threads of a solve pool each
+    own a context and stream), else the process-wide one."""
     global _default
+    ctx = getattr(_local, "ctx", None)
+    if ctx is not None:
+        return ctx
     if _default is None:
         _default = Context()
     return _default
 
 
 def set_default_context(ctx):
+    """Process-wide default context (the main thread's)."""
     global _default
     _default = ctx
+
+
+def device_free_bytes(device=0):
+    """Free device memory in bytes (cudaMemGetInfo)."""
+    L = lib()
+    f, t = u64(), u64()
+    rc = L.nsg_device_memory(int(device), C.byref(f), C.byref(t))
+    if rc != 0:
+        raise RuntimeError(f"nsg_device_memory failed ({rc})")
+    return int(f.value)
+
+
+def set_thread_context(ctx):
+    """Default context of the calling thread only (None clears it)."""
+    _local.ctx = ctx

@@ -222,6 +222,19 @@ int nsg_ctx_profile_read(nsg_ctx* c, int cls, uint64_t* launches, double* ms, do
   NSG_API_END(c)
 }
 
+int nsg_device_memory(int device, uint64_t* free_bytes, uint64_t* total_bytes) {
+  int prev = 0;
+  if (cudaGetDevice(&prev) != cudaSuccess) return NSG_ERR_CUDA;
+  if (cudaSetDevice(device) != cudaSuccess) return NSG_ERR_CUDA;
+  size_t f = 0, t = 0;
+  cudaError_t e = cudaMemGetInfo(&f, &t);
+  cudaSetDevice(prev);
+  if (e != cudaSuccess) return NSG_ERR_CUDA;
+  if (free_bytes) *free_bytes = f;
+  if (total_bytes) *total_bytes = t;
+  return NSG_OK;
+}
+
 int nsg_ctx_memory(const nsg_ctx* c, uint64_t* in_use, uint64_t* peak, uint64_t* budget) {
   if (!c) return NSG_ERR_INVALID;
   if (in_use) *in_use = c->in_use;

@@ -435,11 +435,12 @@ bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
   slice_operand<S>(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
   CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM, S), mB = make_map(Bs, Np, Kp, S * bb, BN, S);
   int* err = device_flag(c);  // checked once at the end of the public call
-  static bool attr = false;  // one flag per instantiation
-  if (!attr) {
-    NSG_CUDA(cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
+  static std::once_flag attr;  // one per instantiation; contexts on other threads race here
+  cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr, [&] {
+    attr_err = cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
+  NSG_CUDA(attr_err);
   OzEpi ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, sa, sb, Mp, Np,
            ab > 1, bb > 1, err};
   dim3 grid(unsigned(Mp / BM), unsigned(Np / BN), unsigned(g.batch));

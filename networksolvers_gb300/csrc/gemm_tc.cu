@@ -391,11 +391,12 @@ bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g) {
   CUtensorMap mBh = make_map(Bh, Np, Kp, bb, BN), mBl = make_map(Bl, Np, Kp, bb, BN);
   int* err = (int*)dev_scratch(c, 1);  // first slot of the reduction scratch
   NSG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-  static bool attr = false;
-  if (!attr) {
-    NSG_CUDA(cudaFuncSetAttribute(tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr = true;
-  }
+  static std::once_flag attr;  // contexts on other threads race here
+  cudaError_t attr_err = cudaSuccess;
+  std::call_once(attr, [&] {
+    attr_err = cudaFuncSetAttribute(tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+  });
+  NSG_CUDA(attr_err);
   EpiParams ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, err};
   if (g.batch > 1 && (ab == 1 || bb == 1)) {
     // a batch with one operand shared (the small operator tensors) stays on the FP64 path

@@ -19,11 +19,26 @@
 #include <algorithm>
 #include <cmath>
 #include <functional>
+#include <map>
+#include <mutex>
 #include <numeric>
 
 namespace nsg {
 
 void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* w);  // eig.cu
+
+// Raise a kernel's dynamic shared-memory limit, never lower it.  The attribute is
+// process-wide and contexts on other host threads launch the same kernels concurrently
+// with other sizes: a limit lowered by one of them would fail another's launch.
+static void raise_smem_limit(const void* fn, int bytes) {
+  static std::mutex mu;
+  static std::map<const void*, int> limit;
+  std::lock_guard<std::mutex> g(mu);
+  int& cur = limit[fn];
+  if (bytes <= cur) return;
+  NSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
+}
 
 namespace {
 
@@ -1181,7 +1196,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
     for (auto& m : lv) maxnb = std::max(maxnb, m.hi - m.lo);
     if (maxnb <= kSmemMerge) {
       const int shm = maxnb * (6 * 8);
-      NSG_CUDA(cudaFuncSetAttribute(merge_prep_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+      raise_smem_limit((const void*)merge_prep_smem_kernel, shm);
       merge_prep_smem_kernel<<<nm, 256, shm, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
     } else {
       merge_prep_kernel<<<nm, 32, 0, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
@@ -1205,8 +1220,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       DevBuf Qk(c, sizeof(double) * (size_t)nb * std::max(k, 1)), Qm(c, sizeof(double) * (size_t)nb * std::max(k, 1));
       if (nb <= kSmemMerge) {
         const int shm = nb * 8;
-        NSG_CUDA(cudaFuncSetAttribute(gather_nondeflated_smem_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      shm));
+        raise_smem_limit((const void*)gather_nondeflated_smem_kernel, shm);
         gather_nondeflated_smem_kernel<<<1, 256, shm, c->stream>>>(nb, W.kind + M.lo, W.Ds + M.lo, W.zs + M.lo,
                                                                    kpos.as<int>(), Dk.as<double>(), zk.as<double>());
       } else {
@@ -1214,6 +1228,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
                                                            W.Ds + M.lo, W.zs + M.lo, kpos.as<int>(), Qk.as<double>(),
                                                            Dk.as<double>(), zk.as<double>());
       }
+      check_launch("dc gather");  // kpos indexes the next kernels: fail before they run
       int gblocks = int(std::min<size_t>(((size_t)nb * nb + 255) / 256, (size_t)c->num_sms * 8));
       gather_cols_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, kpos.as<int>(),
                                                          Qk.as<double>());
@@ -1250,8 +1265,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
           Qnew(c, sizeof(double) * (size_t)nb * nb);
       if (nb <= kSmemMerge) {
         const int shm = nb * (3 * 8 + 3 * 4);
-        NSG_CUDA(cudaFuncSetAttribute(merge_finalize_order_smem_kernel,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+        raise_smem_limit((const void*)merge_finalize_order_smem_kernel, shm);
         merge_finalize_order_smem_kernel<<<1, 256, shm, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(),
                                                                      nb, flip, skind.as<int>(), sidx.as<int>(),
                                                                      wnew.as<double>());
@@ -1259,6 +1273,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
         merge_finalize_order_kernel<<<1, 32, 0, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(), nb, flip,
                                                              skind.as<int>(), sidx.as<int>(), wnew.as<double>());
       }
+      check_launch("dc order");  // src_kind / src_idx index the scatter
       merge_scatter_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, Qm.as<double>(),
                                                            skind.as<int>(), sidx.as<int>(), Qnew.as<double>());
       copy_block_kernel<<<gblocks, 256, 0, c->stream>>>(Qnew.as<double>(), nb, Q, n, M.lo, wnew.as<double>(), w);
@@ -1307,7 +1322,7 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
   gemm_f64_simt(c, g);
   {
     const int shm = int(2 * NB * (NB + 1) * eb);
-    NSG_CUDA(cudaFuncSetAttribute(wy_tfactor_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, shm));
+    raise_smem_limit((const void*)wy_tfactor_kernel<T>, shm);
     wy_tfactor_kernel<T><<<nblk, NB, shm, c->stream>>>(S.as<T>(), taup.as<T>(), Tm.as<T>());
   }
   count_launch(c);
@@ -1389,7 +1404,7 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
     // then spread over all SMs; wider CTAs and two CTAs per SM measured slower
     constexpr int kTriThreads = 256;
     auto kfn = tridiag_kernel<T, kTriThreads>;
-    NSG_CUDA(cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(shm)));
+    raise_smem_limit((const void*)kfn, int(shm));
     NSG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&max_blocks, kfn, kTriThreads, shm));
     NSG_CHECK(max_blocks > 0, NSG_ERR_UNSUPPORTED, "tridiagonalisation: no resident block fits");
     int64_t want = ((int64_t)n * n + kTriThreads * 8 - 1) / (kTriThreads * 8);
