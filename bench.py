@@ -296,6 +296,154 @@ def run_nsg(args):
         td.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# further workloads (one JSON line each; the default is the N=100 DMRG benchmark)
+# ---------------------------------------------------------------------------
+
+
+def _line(**kw):
+    base = {"n_gpus": 1, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "data": "synthetic"}
+    base.update(kw)
+    print(json.dumps(base), flush=True)
+
+
+def run_tdvp(args):
+    """2-site TDVP on the depth-5 binary-tree TFIM (63 sites, d=2, complex128): all-up
+    start, dt = 0.05, maxdim 256, cutoff 1e-9, Krylov exponential tol 1e-12.  One step =
+    one time step (a 4th-order TDVP sweep).  The split form is timed over steps
+    W+1..W+K and compared with the plain form over the same steps (fidelity of the two
+    final states)."""
+    import networksolvers_gb300.models as m
+    from networksolvers_gb300 import _native
+    from networksolvers_gb300.network import inner
+    from networksolvers_gb300.sweep import ApplyExpProblem, exponentiate_solver, sweep_solve, updater_applyexp
+    from networksolvers_gb300.network import tdvp_regions
+    ctx = _native.Context(0, precision="fp64")
+    _native.set_default_context(ctx)
+    g = m.binary_tree_graph(5)
+    H = m.tfim_tree(g, h=1.0).astype(np.complex128)
+    psi0 = m.all_up_state(g)
+    trunc = dict(cutoff=1e-9, maxdim=256)
+    total = args.warmup + args.steps
+    from networksolvers_gb300.network import ProjTTN, from_network
+    out = {}
+    sites = {}  # both runs share the site indices, so their final states can be overlapped
+    for prec in ("fp64", args.precision):
+        ctx.set_precision(prec)
+        psi, _ = from_network(psi0, site_index=sites, ctx=ctx, dtype=np.complex128)
+        (gh, Ht), _ = from_network(H, site_index=sites, ctx=ctx, dtype=np.complex128)
+        P = ProjTTN(psi.g, Ht)
+        prob = ApplyExpProblem(psi, P)
+        ms = []
+        for step in range(total):
+            plan = tdvp_regions(psi.g, -1j * 0.05, updater_kwargs=dict(solver=exponentiate_solver, tol=1e-12),
+                                tdvp_order=4, nsites=2, inserter_kwargs=dict(trunc=trunc))
+            ctx.synchronize()
+            ctx.record(0)
+            prob = sweep_solve(prob, [plan], updater_applyexp)
+            ctx.record(1)
+            ms.append(ctx.elapsed_ms(0, 1))
+        out[prec] = (prob.state, ms[args.warmup:], prob.state.maxlinkdim())
+    a, b = out["fp64"][0], out[args.precision][0]
+    ab, aa, bb = inner(a, b), inner(a, a), inner(b, b)
+    fid = abs(ab) ** 2 / (abs(aa) * abs(bb))
+    t = float(np.sum(out[args.precision][1])) / 1e3
+    tp = float(np.sum(out["fp64"][1])) / 1e3
+    _line(metric="tdvp_steps_per_s", value=args.steps / t, unit="steps/s", steps=args.steps, warmup=args.warmup,
+          ms_per_step=t * 1e3 / args.steps, dtype=f"c128 ({args.precision})",
+          config={"workload": "tfim_binary_tree_depth5_2site_tdvp", "sites": 63, "dt": 0.05, "maxdim": 256,
+                  "cutoff": 1e-9, "timed_steps": list(range(args.warmup + 1, total + 1))},
+          plain_fp64={"value": args.steps / tp, "unit": "steps/s"}, split_vs_plain=tp / t,
+          fidelity_split_vs_plain=fid, maxlinkdim=out[args.precision][2])
+
+
+def _pool_jobs_c4(count):
+    import networksolvers_gb300.models as m
+    from networksolvers_gb300 import batch
+    jobs = []
+    for k in range(count):
+        c = m.config_j1j2_batch(k)
+        jobs.append(batch.dmrg_job(c["H"], c["psi0"], tag=k, nsweeps=6, maxdim=c["maxdim"], cutoff=1e-10))
+    return jobs
+
+
+def run_batch(args):
+    """256 independent J1-J2 chains (seed k: N~U[16,64], J2~U[0,0.5], maxdim~U{32,64,128},
+    random MPS bond dimension 8, 6 sweeps, cutoff 1e-10) advanced concurrently by a pool
+    of workers (one context and stream each), against sequential plain FP64 solves of
+    the first --sample chains (the same chains' energies give the accuracy)."""
+    from networksolvers_gb300 import batch
+    jobs = _pool_jobs_c4(args.chains)
+    t0 = time.perf_counter()
+    seq = batch.SolvePool(workers=1, precision="fp64").run(jobs[:args.sample])
+    t_seq = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res = batch.SolvePool(workers=args.workers, precision=args.precision).run(jobs)
+    t_pool = time.perf_counter() - t0
+    err = [r.error for r in res + seq if r.error]
+    dE = max(abs(r.value - q.value) / abs(q.value) for r, q in zip(res, seq))
+    v = len(res) / t_pool
+    _line(metric="batched_dmrg_solves_per_s", value=v, unit="solves/s", steps=1, warmup=0,
+          ms_per_step=t_pool * 1e3, dtype=f"f64 ({args.precision})",
+          config={"workload": "j1j2_chain_batch", "chains": len(jobs), "workers": args.workers,
+                  "nsweeps": 6, "cutoff": 1e-10},
+          sequential_fp64={"value": args.sample / t_seq, "unit": "solves/s", "sample": f"chains 0..{args.sample - 1}"},
+          speedup_vs_sequential=v / (args.sample / t_seq), max_rel_dE_vs_sequential=dE, errors=err[:3])
+
+
+def _serve_jobs(rate, duration, seed):
+    import networksolvers_gb300.models as m
+    from networksolvers_gb300 import batch
+    arr = batch.poisson_arrivals(rate, duration, seed)
+    rng = np.random.Generator(np.random.PCG64(seed + 1))
+    jobs = []
+    for i, t in enumerate(arr):
+        if rng.uniform() < 0.7:
+            n = int(rng.integers(20, 129))
+            delta = float(rng.uniform(0.0, 2.0))
+            md = int(rng.choice([64, 128, 256]))
+            H = m.xxz_chain(n, delta)
+            psi0 = m.random_state(m.chain_graph(n), 8, seed=seed * 100003 + i)
+            jobs.append(batch.dmrg_job(H, psi0, tag=("dmrg", i), arrival=t, nsweeps=5, maxdim=md, cutoff=1e-10))
+        else:
+            depth = int(rng.integers(3, 6))
+            h = float(rng.uniform(0.5, 1.5))
+            g = m.binary_tree_graph(depth)
+            H = m.tfim_tree(g, h=h).astype(np.complex128)
+            jobs.append(batch.tdvp_job(H, m.all_up_state(g), [0.05 * (k + 1) for k in range(20)], tag=("tdvp", i),
+                                       arrival=t, maxdim=64))
+    return jobs
+
+
+def run_serve(args):
+    """Serving stream: Poisson arrivals at --rate req/s for --duration s (seeded), 70 %
+    ground-state DMRG on XXZ chains (N~U[20,128], Delta~U[0,2], maxdim~U{64,128,256},
+    5 sweeps, cutoff 1e-10), 30 % TDVP quenches of binary-tree TFIM (depth 3-5,
+    h~U[0.5,1.5], 20 steps of dt=0.05, maxdim 64).  Admission by HBM footprint;
+    p50 / p99 latency and solves/s, against sequential plain FP64 solves of the first
+    --sample requests."""
+    from networksolvers_gb300 import batch
+    jobs = _serve_jobs(args.rate, args.duration, args.seed)
+    t0 = time.perf_counter()
+    seq = batch.SolvePool(workers=1, precision="fp64").run(
+        [batch.Job(j.kind, j.H, j.psi0, j.kwargs, j.tag, 0.0) for j in jobs[:args.sample]])
+    t_seq = time.perf_counter() - t0
+    res = batch.SolvePool(workers=args.workers, precision=args.precision).run(jobs)
+    summ = batch.latency_summary(res)
+    same = []
+    for r, q in zip(res, seq):
+        if r.kind == "dmrg" and r.error is None and q.error is None:
+            same.append(abs(r.value - q.value) / abs(q.value))
+    _line(metric="served_solves_per_s", value=summ["solves_per_s"], unit="solves/s", steps=1, warmup=0,
+          ms_per_step=summ["span_s"] * 1e3, dtype=f"f64/c128 ({args.precision})",
+          config={"workload": "serve_xxz_dmrg_tfim_tdvp_mix", "rate_per_s": args.rate, "duration_s": args.duration,
+                  "requests": len(jobs), "workers": args.workers},
+          latency={"p50_s": summ["p50_s"], "p99_s": summ["p99_s"]}, failed=summ["failed"],
+          sequential_fp64={"value": args.sample / t_seq, "unit": "solves/s",
+                           "sample": f"requests 0..{args.sample - 1}"},
+          max_rel_dE_vs_sequential=max(same) if same else None)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,11 +453,26 @@ def main():
     ap.add_argument("--precision", default="ozaki", choices=["ozaki", "tf32x3", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "tdvp", "batch", "serve"],
+                    help="dmrg: the N=100 benchmark (default); tdvp: binary-tree TFIM TDVP; batch: 256 "
+                         "J1-J2 chains on a solve pool; serve: Poisson request stream")
+    ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--chains", type=int, default=256)
+    ap.add_argument("--sample", type=int, default=16)
+    ap.add_argument("--rate", type=float, default=1.0)
+    ap.add_argument("--duration", type=float, default=30.0)
+    ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
-    if args.warmup < 3:
+    if args.warmup < 3 and args.workload in ("dmrg", "tdvp"):
         raise SystemExit("warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "tdvp":
+        run_tdvp(args)
+    elif args.workload == "batch":
+        run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_nsg(args)
 
