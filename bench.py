@@ -266,6 +266,12 @@ def run_nsg(args):
         roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": None, "kernel": dom,
                 "peak_note": "GB300 FP64 rate (no FP64 figure in the measured peaks; 1.25 TFLOP/s nominal)"}
+        if dom == "tridiag":
+            # DRAM bytes of one launch from the ncu capture at n = 1024 (8.44 MB read + 1.83 MB
+            # written: the L2-resident matrix once, the reflectors back), scaled by n^2 to the
+            # n = 2048 launches of the bond-dimension-1024 regions
+            roof["traffic"] = 10.27e6 * 4.0
+            roof["traffic_note"] = "bytes per n=2048 launch, scaled from ncu at n=1024 (n^2)"
     tc = classes.get("tc_gemm")
     heff_tflops = (tc["flops"] / (tc["ms"] / 1e3) / 1e12) if tc else None
     cpu = None

@@ -22,6 +22,8 @@ __device__ __forceinline__ double2 ld(const double2* p, bool conj) {
   return v;
 }
 __device__ __forceinline__ void zero(double& v) { v = 0.0; }
+__device__ __forceinline__ bool nonzero(double v) { return v != 0.0; }
+__device__ __forceinline__ bool nonzero(double2 v) { return v.x != 0.0 || v.y != 0.0; }
 __device__ __forceinline__ void zero(double2& v) { v = make_double2(0.0, 0.0); }
 __device__ __forceinline__ void mac(double& acc, double a, double b) { acc = fma(a, b, acc); }
 __device__ __forceinline__ void mac(double2& acc, double2 a, double2 b) {
@@ -202,12 +204,18 @@ __global__ void __launch_bounds__(256, 1)
           zero(a[u]);
           if (k0 + u < K) a[u] = ld(Ab + i + (int64_t)(k0 + u) * lda, conjA);
         }
+        // op(B) is the fused site operator of the region: mostly zeros.  The test on the
+        // shared value is uniform across the warp, so skipping them saves FP64 work
+        // without divergence.
 #pragma unroll
         for (int u = 0; u < 8; ++u)
           if (k0 + u < K)
 #pragma unroll
             for (int j = 0; j < 32; ++j)
-              if (j < N) mac(acc[j], a[u], Bs[k0 + u][j]);
+              if (j < N) {
+                const T bv = Bs[k0 + u][j];
+                if (nonzero(bv)) mac(acc[j], a[u], bv);
+              }
       }
 #pragma unroll
       for (int j = 0; j < 32; ++j)

@@ -136,3 +136,35 @@ def test_c3_style_schedule_with_densitymatrix(nsg_ctx, precision):
         assert np.array_equal(r[:, 3], ro[:, 3])
         assert np.max(np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])) < 1e-10
     assert abs(E - Eo) / abs(Eo) < (1e-10 if precision == "fp64" else 1e-5)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("model", ["j1j2", "xxz"])
+def test_batch_and_serve_chains_match_oracle(nsg_ctx, model, precision):
+    """The chain families of the batched and served workloads (J1-J2 with its w=8 MPO,
+    XXZ at anisotropy 1.7) against the oracle: per-region energies 1e-10 relative and
+    identical truncated bond dimensions, in the plain and the split form."""
+    from oracle import sweep as osw
+    n = 14
+    H = m.j1j2_chain(n, 0.35) if model == "j1j2" else m.xxz_chain(n, 1.7)
+    psi0 = m.random_state(m.chain_graph(n), 8, seed=3)
+    kw = dict(nsweeps=3, nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+              inserter_kwargs=dict(trunc=dict(cutoff=1e-10, maxdim=32)))
+    got, ref = [], []
+
+    def cb_got(prob, sweep, region, which, **k):
+        got.append((prob.eigenvalue, prob.last_insert.get("newdim", -1)))
+
+    def cb_ref(prob, sweep, region, which, **k):
+        ref.append((prob.eigenvalue, prob.last_insert.get("newdim", -1)))
+
+    nsg_ctx.set_precision(precision)
+    try:
+        E, _ = ns.dmrg(H, psi0, region_callback=cb_got, **kw)
+    finally:
+        nsg_ctx.set_precision("fp64")
+    Eo, _ = osw.dmrg(H, psi0, region_callback=cb_ref, **kw)
+    got, ref = np.array(got), np.array(ref)
+    assert np.array_equal(got[:, 1], ref[:, 1])
+    assert np.max(np.abs(got[:, 0] - ref[:, 0]) / np.abs(ref[:, 0])) < 1e-10
+    assert abs(E - Eo) / abs(Eo) < 1e-10
