@@ -8,6 +8,8 @@
 #include "nsg_internal.h"
 
 #include <algorithm>
+#include <map>
+#include <mutex>
 
 namespace nsg {
 
@@ -171,60 +173,79 @@ __global__ void splitk_reduce_kernel(int64_t M, int64_t N, int64_t batch, int sp
   }
 }
 
-// Tall-skinny products with N, K <= 32 (the site-operator step of H_eff: M = chi, K and N
-// = w d^2, batched over the other bond): one thread per row of C, op(B) staged in
-// shared memory, exactly M N K multiply-adds (the 64x64 tile kernel would pad N and K).
+// Tall-skinny products with N, K <= 32: the site-operator steps of H_eff and of the
+// environment updates (K, N = w d, batched over the other bond).  op(B) is an MPO
+// tensor and mostly zeros, so each CTA lists its non-zeros per column (warp ballots)
+// and stages a 256-row tile of op(A) in shared memory ([k][row], conflict-free); thread
+// r then forms row r of C from exactly nnz(B) multiply-adds.  The FP64 work drops by
+// the operator's sparsity and the kernel runs at the HBM rate of reading A and writing C.
+constexpr int kSkinnyRows = 256;
 template <typename T>
-__global__ void __launch_bounds__(256, 1)
+__global__ void __launch_bounds__(kSkinnyRows)
     gemm_skinny_kernel(int64_t M, int N, int K, const T* __restrict__ A, int64_t lda, int64_t sA, bool conjA,
                        const T* __restrict__ B, int64_t ldb, int64_t sB, int opB, T* __restrict__ C,
                        int64_t ldc, int64_t sC, int64_t batch, Scal<T> sc) {
-  __shared__ T Bs[32][33];
+  extern __shared__ __align__(16) unsigned char sk_smem[];
+  T* As = (T*)sk_smem;                        // [K][kSkinnyRows]
+  __shared__ T nzv[32 * 32];                  // non-zeros of op(B), column-major order
+  __shared__ unsigned char nzk[32 * 32];      // their row index k
+  __shared__ int colptr[33];
   const bool transB = (opB == OP_T || opB == OP_C), conjB = (opB == OP_C || opB == OP_R);
-  for (int64_t bz = blockIdx.y; bz < batch; bz += gridDim.y) {
-    __syncthreads();
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t tiles = (M + kSkinnyRows - 1) / kSkinnyRows;
+  for (int64_t job = blockIdx.x; job < tiles * batch; job += gridDim.x) {
+    const int64_t bz = job / tiles, i0 = (job % tiles) * kSkinnyRows;
     const T* Bb = B + bz * sB;
-    for (int e = threadIdx.x; e < K * N; e += blockDim.x) {
-      const int k = e % K, j = e / K;
-      Bs[k][j] = ld(transB ? Bb + j + (int64_t)k * ldb : Bb + k + (int64_t)j * ldb, conjB);
+    const T* Ab = A + bz * sA;
+    __syncthreads();  // the previous job's readers are done
+    if (warp == 0) {
+      int base = 0;
+      for (int j = 0; j < N; ++j) {
+        T v;
+        zero(v);
+        if (lane < K) v = ld(transB ? Bb + j + (int64_t)lane * ldb : Bb + lane + (int64_t)j * ldb, conjB);
+        const unsigned m = __ballot_sync(0xffffffffu, nonzero(v));
+        if (lane == 0) colptr[j] = base;
+        if (nonzero(v)) {
+          const int pos = base + __popc(m & ((1u << lane) - 1u));
+          nzv[pos] = v;
+          nzk[pos] = (unsigned char)lane;
+        }
+        base += __popc(m);
+      }
+      if (lane == 0) colptr[N] = base;
+    }
+    const int64_t i = i0 + tid;
+    for (int k = 0; k < K; ++k) {
+      T a;
+      zero(a);
+      if (i < M) a = ld(Ab + i + (int64_t)k * lda, conjA);
+      As[k * kSkinnyRows + tid] = a;
     }
     __syncthreads();
-    const T* Ab = A + bz * sA;
-    T* Cb = C + bz * sC;
-    for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < M; i += int64_t(gridDim.x) * blockDim.x) {
-      T acc[32];
-#pragma unroll
-      for (int j = 0; j < 32; ++j) zero(acc[j]);
-      // eight rows of op(A) in flight per thread (the loads, not the FP64 work, set the
-      // latency of this kernel)
-      for (int k0 = 0; k0 < K; k0 += 8) {
-        T a[8];
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          zero(a[u]);
-          if (k0 + u < K) a[u] = ld(Ab + i + (int64_t)(k0 + u) * lda, conjA);
-        }
-        // op(B) is the fused site operator of the region: mostly zeros.  The test on the
-        // shared value is uniform across the warp, so skipping them saves FP64 work
-        // without divergence.
-#pragma unroll
-        for (int u = 0; u < 8; ++u)
-          if (k0 + u < K)
-#pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if (j < N) {
-                const T bv = Bs[k0 + u][j];
-                if (nonzero(bv)) mac(acc[j], a[u], bv);
-              }
+    if (i < M) {
+      T* Cb = C + bz * sC + i;
+      for (int j = 0; j < N; ++j) {
+        T acc;
+        zero(acc);
+        for (int t = colptr[j]; t < colptr[j + 1]; ++t) mac(acc, As[nzk[t] * kSkinnyRows + tid], nzv[t]);
+        T* cp = Cb + (int64_t)j * ldc;
+        *cp = sc.epi(acc, cp);
       }
-#pragma unroll
-      for (int j = 0; j < 32; ++j)
-        if (j < N) {
-          T* cp = Cb + i + (int64_t)j * ldc;
-          *cp = sc.epi(acc[j], cp);
-        }
     }
   }
+}
+
+// Raise a kernel's dynamic shared-memory limit once per process (set to the most any
+// call can ask for, so concurrent contexts never see a lower one).
+void raise_smem_limit_gemm(const void* fn, int bytes) {
+  static std::mutex mu;
+  static std::map<const void*, int> limit;
+  std::lock_guard<std::mutex> lk(mu);
+  int& cur = limit[fn];
+  if (bytes <= cur) return;
+  NSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
 }
 
 }  // namespace
@@ -233,23 +254,24 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   if (g.M == 0 || g.N == 0 || g.batch == 0) return;
   if (g.N <= 32 && g.K <= 32 && g.K >= 1 && (g.opA == OP_N || g.opA == OP_R)) {
     const int64_t sms = c->num_sms > 0 ? c->num_sms : 152;
-    const int64_t rows_blocks = (g.M + 255) / 256;
-    const int64_t gb = std::min<int64_t>(g.batch, 65535);
-    const int64_t gx = std::max<int64_t>(1, std::min<int64_t>(rows_blocks, (sms * 8 + gb - 1) / gb));
-    dim3 grid{unsigned(gx), unsigned(gb), 1};
+    const int64_t jobs = ((g.M + kSkinnyRows - 1) / kSkinnyRows) * g.batch;
+    const int grid = int(std::min<int64_t>(jobs, sms * 16));
     ProfScope ps(c, NSG_PROF_SIMT_GEMM,
                  double(g.M) * double(g.N) * double(g.K) * double(g.batch) * (g.dtype == NSG_C128 ? 8.0 : 2.0));
     if (g.dtype == NSG_C128) {
+      const int shm = int(g.K) * kSkinnyRows * 16;
       Scal<double2> sc{make_double2(g.alpha_re, g.alpha_im), make_double2(g.beta_re, g.beta_im)};
-      gemm_skinny_kernel<double2><<<grid, 256, 0, c->stream>>>(
+      raise_smem_limit_gemm((const void*)gemm_skinny_kernel<double2>, 32 * kSkinnyRows * 16);
+      gemm_skinny_kernel<double2><<<grid, kSkinnyRows, shm, c->stream>>>(
           g.M, int(g.N), int(g.K), (const double2*)g.A, g.lda, g.strideA, g.opA == OP_R, (const double2*)g.B,
           g.ldb, g.strideB, g.opB, (double2*)g.C, g.ldc, g.strideC, g.batch, sc);
     } else {
+      const int shm = int(g.K) * kSkinnyRows * 8;
       Scal<double> sc{g.alpha_re, g.beta_re};
-      gemm_skinny_kernel<double><<<grid, 256, 0, c->stream>>>(g.M, int(g.N), int(g.K), (const double*)g.A, g.lda,
-                                                              g.strideA, false, (const double*)g.B, g.ldb,
-                                                              g.strideB, g.opB, (double*)g.C, g.ldc, g.strideC,
-                                                              g.batch, sc);
+      raise_smem_limit_gemm((const void*)gemm_skinny_kernel<double>, 32 * kSkinnyRows * 8);
+      gemm_skinny_kernel<double><<<grid, kSkinnyRows, shm, c->stream>>>(
+          g.M, int(g.N), int(g.K), (const double*)g.A, g.lda, g.strideA, false, (const double*)g.B, g.ldb,
+          g.strideB, g.opB, (double*)g.C, g.ldc, g.strideC, g.batch, sc);
     }
     count_launch(c);
     check_launch("gemm_skinny");
