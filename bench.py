@@ -313,6 +313,54 @@ def _line(**kw):
     print(json.dumps(base), flush=True)
 
 
+def _oracle_sweep_seconds(run, first, count):
+    """CPU baseline leg: run an oracle driver with a sweep callback and return the wall
+    time of sweeps first..first+count-1 (1-based), on all host threads."""
+    stamps = []
+    t0 = time.perf_counter()
+    run(lambda prob, sweep, **k: stamps.append(time.perf_counter()))
+    marks = [t0] + stamps
+    return marks[first - 1 + count] - marks[first - 1]
+
+
+def run_c1(args):
+    """The reference's own CPU-runnable case: Heisenberg N=20, random MPS bond dimension
+    10 from seed 0, 2-site DMRG, maxdim 64, cutoff 1e-10, Lanczos krylovdim 3 / maxiter 1.
+    One step = one sweep (W warm-up sweeps, K timed)."""
+    import networksolvers_gb300 as ns
+    import networksolvers_gb300.models as m
+    from networksolvers_gb300 import _native
+    ctx = _native.Context(0, precision=args.precision)
+    _native.set_default_context(ctx)
+    H, psi0 = m.config_heisenberg_chain(20, 10, 0)
+    kw = dict(nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+              inserter_kwargs=dict(trunc=dict(cutoff=1e-10, maxdim=64)))
+    total = args.warmup + args.steps
+    marks = []
+    ctx.synchronize()
+
+    def cb(prob, sweep, **k):
+        ctx.record(sweep % 2)
+        ctx.synchronize()
+        marks.append(time.perf_counter())
+
+    t0 = time.perf_counter()
+    E, _ = ns.dmrg(H, psi0, nsweeps=total, sweep_callback=cb, **kw)
+    marks = [t0] + marks
+    t = marks[total] - marks[args.warmup]
+    cpu = None
+    if not args.no_cpu:
+        from oracle import sweep as osw
+        tc = _oracle_sweep_seconds(lambda cbk: osw.dmrg(H, psi0, nsweeps=total, sweep_callback=cbk, **kw),
+                                   args.warmup + 1, args.steps)
+        cpu = {"value": args.steps / tc, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the same run, sweeps {args.warmup + 1}-{total}"}
+    _line(metric="dmrg_sweeps_per_s", value=args.steps / t, unit="sweeps/s", steps=args.steps, warmup=args.warmup,
+          ms_per_step=t * 1e3 / args.steps, dtype="f64" if args.precision == "fp64" else f"{args.precision}+f64",
+          config={"workload": "heisenberg_chain_N20_2site_dmrg_maxdim64", "timing": "host clock around synchronised sweeps"},
+          energy=E, cpu_baseline=cpu)
+
+
 def run_tdvp(args):
     """2-site TDVP on the depth-5 binary-tree TFIM (63 sites, d=2, complex128): all-up
     start, dt = 0.05, maxdim 256, cutoff 1e-9, Krylov exponential tol 1e-12.  One step =
@@ -350,6 +398,16 @@ def run_tdvp(args):
             ctx.record(1)
             ms.append(ctx.elapsed_ms(0, 1))
         out[prec] = (prob.state, ms[args.warmup:], prob.state.maxlinkdim())
+    cpu = None
+    if not args.no_cpu:
+        from oracle import sweep as osw
+        exps = [-1j * 0.05 * k for k in range(total + 1)]
+        tc = _oracle_sweep_seconds(
+            lambda cbk: osw.applyexp(H, psi0, exps, nsites=2, sweep_callback=cbk,
+                                     updater_kwargs=dict(solver=osw.exponentiate_solver, tol=1e-12),
+                                     inserter_kwargs=dict(trunc=trunc)), args.warmup + 1, args.steps)
+        cpu = {"value": args.steps / tc, "unit": "steps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the same run, steps {args.warmup + 1}-{total}"}
     a, b = out["fp64"][0], out[args.precision][0]
     ab, aa, bb = inner(a, b), inner(a, a), inner(b, b)
     fid = abs(ab) ** 2 / (abs(aa) * abs(bb))
@@ -360,7 +418,7 @@ def run_tdvp(args):
           config={"workload": "tfim_binary_tree_depth5_2site_tdvp", "sites": 63, "dt": 0.05, "maxdim": 256,
                   "cutoff": 1e-9, "timed_steps": list(range(args.warmup + 1, total + 1))},
           plain_fp64={"value": args.steps / tp, "unit": "steps/s"}, split_vs_plain=tp / t,
-          fidelity_split_vs_plain=fid, maxlinkdim=out[args.precision][2])
+          fidelity_split_vs_plain=fid, maxlinkdim=out[args.precision][2], cpu_baseline=cpu)
 
 
 def _pool_jobs_c4(count):
@@ -389,12 +447,24 @@ def run_batch(args):
     err = [r.error for r in res + seq if r.error]
     dE = max(abs(r.value - q.value) / abs(q.value) for r, q in zip(res, seq))
     v = len(res) / t_pool
+    cpu = None
+    if not args.no_cpu:
+        from oracle import sweep as osw
+        t0 = time.perf_counter()
+        ncpu = 2
+        for j in jobs[:ncpu]:
+            kw = dict(j.kwargs)
+            osw.dmrg(j.H, j.psi0, kw.pop("nsweeps"), **kw)
+        tc = time.perf_counter() - t0
+        cpu = {"value": ncpu / tc, "unit": "solves/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": "chains 0-1, sequential"}
     _line(metric="batched_dmrg_solves_per_s", value=v, unit="solves/s", steps=1, warmup=0,
           ms_per_step=t_pool * 1e3, dtype=f"f64 ({args.precision})",
           config={"workload": "j1j2_chain_batch", "chains": len(jobs), "workers": args.workers,
                   "nsweeps": 6, "cutoff": 1e-10},
           sequential_fp64={"value": args.sample / t_seq, "unit": "solves/s", "sample": f"chains 0..{args.sample - 1}"},
-          speedup_vs_sequential=v / (args.sample / t_seq), max_rel_dE_vs_sequential=dE, errors=err[:3])
+          speedup_vs_sequential=v / (args.sample / t_seq), max_rel_dE_vs_sequential=dE, errors=err[:3],
+          cpu_baseline=cpu)
 
 
 def _serve_jobs(rate, duration, seed):
@@ -459,9 +529,9 @@ def main():
     ap.add_argument("--precision", default="ozaki", choices=["ozaki", "tf32x3", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "tdvp", "batch", "serve"],
-                    help="dmrg: the N=100 benchmark (default); tdvp: binary-tree TFIM TDVP; batch: 256 "
-                         "J1-J2 chains on a solve pool; serve: Poisson request stream")
+    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve"],
+                    help="dmrg: the N=100 benchmark (default); c1: the N=20 chain; tdvp: binary-tree TFIM "
+                         "TDVP; batch: 256 J1-J2 chains on a solve pool; serve: Poisson request stream")
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--sample", type=int, default=16)
@@ -469,10 +539,12 @@ def main():
     ap.add_argument("--duration", type=float, default=30.0)
     ap.add_argument("--seed", type=int, default=0)
     args = ap.parse_args()
-    if args.warmup < 3 and args.workload in ("dmrg", "tdvp"):
+    if args.warmup < 3 and args.workload in ("dmrg", "c1", "tdvp"):
         raise SystemExit("warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c1":
+        run_c1(args)
     elif args.workload == "tdvp":
         run_tdvp(args)
     elif args.workload == "batch":
