@@ -240,8 +240,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == NDRAIN_WARPS) {
     if (lane == 0) {
       // kind::f16: D F32 (bits 4-5 = 1), A BF16 (7-9 = 1), B BF16 (10-12 = 1), K-major both
-      const uint32_t idesc =
-          (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) | ((uint32_t)(BM >> 4) << 24);
+      // instruction descriptor for an N-wide product (N = 64 .. 256, a multiple of 64 here)
+      const uint32_t idesc0 = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BM >> 4) << 24);
+      auto idesc_n = [&](int n) { return idesc0 | ((uint32_t)(n >> 3) << 17); };
       auto a_ptr = [&](int st, int s) { return smem + st * STAGE_BYTES + s * SLICE_A; };
       auto b_ptr = [&](int st, int s) { return smem + st * STAGE_BYTES + S * SLICE_A + s * SLICE_B; };
       auto issue = [&](int t, int st) {
@@ -271,15 +272,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
           for (int kk = 0; kk < BKS / 16; ++kk) {
             const uint32_t off = kk * 32;  // 16 bf16 = 32 bytes inside the 64-byte swizzle atom
+            // A^(s) meets B^(0..G-1-s) in one product of width (G-s) x BN: the B slices lie
+            // back to back along N in shared memory (8-row groups 512 B apart throughout)
+            // and the accumulators of groups s .. G-1 back to back in TMEM, so D columns
+            // [s BN, G BN) += A^(s) [B^(0) | ... | B^(G-1-s)], split in widths <= 256.
+            // (One 64-wide product per slice pair re-read A from shared memory 21 times.)
 #pragma unroll
-            for (int s = 0; s < S; ++s) {
-              const uint64_t ad = sdesc64(smem_u32(a_ptr(st, s)) + off);
+            for (int sa = 0; sa < S; ++sa) {
+              const uint64_t ad = sdesc64(smem_u32(a_ptr(st, sa)) + off);
 #pragma unroll
-              for (int u = 0; u + s < G; ++u) {
-                const int g = s + u;
-                // group g's first product of the chunk is (s = 0, u = g) at t = t0, kk = 0
-                mma_bf16(tmem + (uint32_t)(g * BN), ad, sdesc64(smem_u32(b_ptr(st, u)) + off), idesc,
-                         (t == t0 && kk == 0 && s == 0) ? 0u : 1u);
+              for (int u0 = 0; u0 < G - sa; u0 += 4) {
+                const int width = (G - sa - u0) >= 4 ? 4 * BN : (G - sa - u0) * BN;
+                // every accumulator's first product of the chunk is the sa = 0 one at t0, kk 0
+                mma_bf16(tmem + (uint32_t)((sa + u0) * BN), ad, sdesc64(smem_u32(b_ptr(st, u0)) + off),
+                         idesc_n(width), (t == t0 && kk == 0 && sa == 0) ? 0u : 1u);
               }
             }
           }
@@ -318,19 +324,32 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         break;
       }
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      // three groups' TMEM loads in flight per wait (one wait per group made the drain,
+      // and with it the tensor pipe, wait on the load latency six times per chunk); the
+      // groups are still added in ascending order
 #pragma unroll
-      for (int g = 0; g < G; ++g) {
-        uint32_t r[16];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, "
-            "%14, %15}, [%16];"
-            : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
-              "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
-            : "r"(tmem + lane_base + (uint32_t)(g * BN + 16 * q)));
+      for (int g0 = 0; g0 < G; g0 += 3) {
+        uint32_t r[3][16];
+#pragma unroll
+        for (int gg = 0; gg < 3; ++gg) {
+          if (g0 + gg < G)
+            asm volatile(
+                "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, "
+                "%13, %14, %15}, [%16];"
+                : "=r"(r[gg][0]), "=r"(r[gg][1]), "=r"(r[gg][2]), "=r"(r[gg][3]), "=r"(r[gg][4]), "=r"(r[gg][5]),
+                  "=r"(r[gg][6]), "=r"(r[gg][7]), "=r"(r[gg][8]), "=r"(r[gg][9]), "=r"(r[gg][10]), "=r"(r[gg][11]),
+                  "=r"(r[gg][12]), "=r"(r[gg][13]), "=r"(r[gg][14]), "=r"(r[gg][15])
+                : "r"(tmem + lane_base + (uint32_t)((g0 + gg) * BN + 16 * q)));
+        }
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        const float sc = __int_as_float((127 - 7 * (g + 2)) << 23);  // 2^{-7(g+2)}, exact
 #pragma unroll
-        for (int j = 0; j < 16; ++j) two_sum_acc(hi[j], lo[j], __uint_as_float(r[j]) * sc);
+        for (int gg = 0; gg < 3; ++gg) {
+          if (g0 + gg < G) {
+            const float sc = __int_as_float((127 - 7 * (g0 + gg + 2)) << 23);  // 2^{-7(g+2)}, exact
+#pragma unroll
+            for (int j = 0; j < 16; ++j) two_sum_acc(hi[j], lo[j], __uint_as_float(r[gg][j]) * sc);
+          }
+        }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       mbar_arrive(accempty);
