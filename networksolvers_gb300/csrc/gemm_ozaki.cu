@@ -192,6 +192,27 @@ struct OzEpi {
   int* err;
 };
 
+// float -> double by exponent re-bias (exact for normal floats; zero, subnormals, inf and
+// NaN take the conversion instruction)
+__device__ __forceinline__ double widen(float f) {
+  const uint32_t b = __float_as_uint(f);
+  const uint32_t e = (b >> 23) & 0xFFu;
+  if (e == 0u || e == 0xFFu) return (double)f;
+  const uint64_t d = ((uint64_t)(b >> 31) << 63) | ((uint64_t)(e + 896u) << 52) | ((uint64_t)(b & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)d);
+}
+// exponent k of a normal power of two 2^k
+__device__ __forceinline__ int pow2_exponent(double p) {
+  return int((__double_as_longlong(p) >> 52) & 0x7FF) - 1023;
+}
+// v * 2^k by adding k to the exponent field when the result stays normal
+__device__ __forceinline__ double scale_pow2(double v, int k) {
+  const long long b = __double_as_longlong(v);
+  const int e = int((b >> 52) & 0x7FF);
+  if (e == 0 || e == 0x7FF || e + k <= 0 || e + k >= 0x7FF) return v * ldexp(1.0, k);
+  return __longlong_as_double(b + ((long long)k << 52));
+}
+
 __device__ __forceinline__ void two_sum_acc(float& hi, float& lo, float x) {
   float s = hi + x;
   float bb = s - hi;
@@ -361,17 +382,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
     }
     if (ok) {
+      // Epilogue with as few FP64-pipe operations as possible (GB300 runs FP64 at ~2 per
+      // clock per SM, and this loop touches every output): the FP32 pair is widened by
+      // exponent arithmetic, added with one DADD, and the power-of-two scales sigma_i tau_j
+      // are applied to the exponent field; alpha = 1 costs nothing further.
       const int64_t row = m0 + wl * 32 + lane;
       if (row < ep.M) {
-        const double sa = ep.sa[(ep.a_batched ? bz : 0) * ep.Mp + row];
+        const int ka = pow2_exponent(ep.sa[(ep.a_batched ? bz : 0) * ep.Mp + row]);
+        const bool unit_alpha = ep.alpha == 1.0;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int64_t col = n0 + 16 * q + j;
           if (col < ep.N) {
-            const double sb = ep.sb[(ep.b_batched ? bz : 0) * ep.Np + col];
-            const double v = ((double)hi[j] + (double)lo[j]) * sa * sb;
+            const int kb = pow2_exponent(ep.sb[(ep.b_batched ? bz : 0) * ep.Np + col]);
+            double v = scale_pow2(widen(hi[j]) + widen(lo[j]), ka + kb);
+            if (!unit_alpha) v *= ep.alpha;
             double* cp = ep.C + bz * ep.sC + row + col * ep.ldc;
-            *cp = (ep.beta == 0.0) ? ep.alpha * v : fma(ep.alpha, v, ep.beta * (*cp));
+            *cp = (ep.beta == 0.0) ? v : fma(ep.beta, *cp, v);
           }
         }
       }
