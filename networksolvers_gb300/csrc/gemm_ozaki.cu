@@ -363,6 +363,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                 : "r"(tmem + lane_base + (uint32_t)((g0 + gg) * BN + 16 * q)));
         }
         asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (g0 + 3 >= G) {
+          // the last loads are in registers: release the accumulators before the
+          // arithmetic, so the next chunk's products overlap it
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          mbar_arrive(accempty);
+        }
 #pragma unroll
         for (int gg = 0; gg < 3; ++gg) {
           if (g0 + gg < G) {
@@ -372,8 +378,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      mbar_arrive(accempty);
 #pragma unroll
       for (int j = 0; j < 16; ++j) {  // renormalise (fast two-sum)
         float s = hi[j] + lo[j];
