@@ -421,6 +421,41 @@ def run_tdvp(args):
           fidelity_split_vs_plain=fid, maxlinkdim=out[args.precision][2], cpu_baseline=cpu)
 
 
+def run_c3_accuracy(args):
+    """The large DMRG configuration run to its full 10 sweeps in the plain and in the split
+    form from the same initial state: the energies of both after every sweep, |dE/E| of
+    the final energies, and the per-sweep times (CUDA events) of each form."""
+    import networksolvers_gb300 as ns
+    from networksolvers_gb300 import _native
+    ctx = _native.Context(0, precision="fp64")
+    _native.set_default_context(ctx)
+    H, psi0 = workload()
+    kw = kwargs_for(0)
+    res = {}
+    for prec in ("fp64", args.precision):
+        ctx.set_precision(prec)
+        ens, ms = [], []
+        ctx.synchronize()
+        ctx.record(0)
+
+        def cb(prob, sweep, **k):
+            ctx.record(1)
+            ms.append(ctx.elapsed_ms(0, 1))
+            ctx.record(0)
+            ens.append(prob.eigenvalue)
+
+        E, psi = ns.dmrg(H, psi0, nsweeps=args.sweeps, sweep_callback=cb, **kw)
+        res[prec] = (ens, ms, psi.maxlinkdim())
+    ep, es = res["fp64"][0], res[args.precision][0]
+    _line(metric="dmrg_energy_agreement", value=abs(es[-1] - ep[-1]) / abs(ep[-1]), unit="|dE/E|",
+          higher_is_better=False, steps=args.sweeps, warmup=0, ms_per_step=float(np.mean(res[args.precision][1])),
+          dtype=f"{args.precision}+f64 vs f64",
+          config={"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "sweeps": args.sweeps,
+                  "maxdim_schedule": SCHEDULE, "cutoff": CUTOFF},
+          energies={"fp64": ep, args.precision: es}, sweep_ms={"fp64": res["fp64"][1], args.precision: res[args.precision][1]},
+          maxlinkdim={"fp64": res["fp64"][2], args.precision: res[args.precision][2]})
+
+
 def _pool_jobs_c4(count):
     import networksolvers_gb300.models as m
     from networksolvers_gb300 import batch
@@ -529,7 +564,7 @@ def main():
     ap.add_argument("--precision", default="ozaki", choices=["ozaki", "tf32x3", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve"],
+    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve", "accuracy"],
                     help="dmrg: the N=100 benchmark (default); c1: the N=20 chain; tdvp: binary-tree TFIM "
                          "TDVP; batch: 256 J1-J2 chains on a solve pool; serve: Poisson request stream")
     ap.add_argument("--workers", type=int, default=16)
@@ -538,6 +573,7 @@ def main():
     ap.add_argument("--rate", type=float, default=1.0)
     ap.add_argument("--duration", type=float, default=30.0)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--sweeps", type=int, default=10)
     args = ap.parse_args()
     if args.warmup < 3 and args.workload in ("dmrg", "c1", "tdvp"):
         raise SystemExit("warmup must be >= 3")
@@ -545,6 +581,8 @@ def main():
         run_reference(args)
     elif args.workload == "c1":
         run_c1(args)
+    elif args.workload == "accuracy":
+        run_c3_accuracy(args)
     elif args.workload == "tdvp":
         run_tdvp(args)
     elif args.workload == "batch":
