@@ -168,3 +168,28 @@ def test_batch_and_serve_chains_match_oracle(nsg_ctx, model, precision):
     assert np.array_equal(got[:, 1], ref[:, 1])
     assert np.max(np.abs(got[:, 0] - ref[:, 0]) / np.abs(ref[:, 0])) < 1e-10
     assert abs(E - Eo) / abs(Eo) < 1e-10
+
+
+def test_split_form_tracks_plain_form_region_by_region(nsg_ctx):
+    """The split form (six-slice tensor-core products; eight-slice in the eigensolver and
+    the expansion) against the plain form along the same sweep: Heisenberg N=24, random MPS
+    chi=16 seed 1, maxdim schedule [32, 64, 128], cutoff 1e-12, densitymatrix expansion.
+    Per-region energies within 1e-10 relative and identical truncated bond dimensions."""
+    H, psi0 = m.heisenberg_chain(24), m.random_state(m.chain_graph(24), 16, seed=1)
+    trunc = dict(cutoff=1e-12, maxdim=[32, 64, 128])
+    kw = dict(nsweeps=3, nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+              extracter_kwargs=dict(trunc=trunc, subspace_algorithm="densitymatrix"),
+              inserter_kwargs=dict(trunc=trunc))
+    Ep, rp, _ = _record_dmrg(ns.dmrg, H, psi0, **kw)
+    nsg_ctx.set_precision("ozaki")
+    nsg_ctx.profile(True)
+    try:
+        Es, rs, _ = _record_dmrg(ns.dmrg, H, psi0, **kw)
+        tc = nsg_ctx.profile_read()["tc_gemm"]["launches"]
+    finally:
+        nsg_ctx.profile(False)
+        nsg_ctx.set_precision("fp64")
+    assert tc > 0  # the tensor-core products did run
+    assert np.array_equal(rs[:, 3], rp[:, 3])
+    assert np.max(np.abs(rs[:, 2] - rp[:, 2]) / np.abs(rp[:, 2])) < 1e-10
+    assert abs(Es - Ep) / abs(Ep) < 1e-10
