@@ -88,6 +88,23 @@ class Clocks:
                 "samples": len(rows)}
 
 
+def replica_time(t_local, device=None):
+    """Slowest replica's time: MAX all-reduce over the process group when one is
+    initialised (the replicas share no data; only this scalar crosses ranks)."""
+    import torch.distributed as td
+    if not (td.is_available() and td.is_initialized()):
+        return t_local
+    import torch
+    tt = torch.tensor([t_local], dtype=torch.float64, device=device or "cpu")
+    td.all_reduce(tt, op=td.ReduceOp.MAX)
+    return float(tt.item())
+
+
+def replica_throughput(world, steps, t_max):
+    """Whole-job throughput of `world` replicas that each ran `steps` steps."""
+    return world * steps / t_max
+
+
 def workload():
     import networksolvers_gb300.models as m
     return m.heisenberg_chain(N_SITES), m.random_state(m.chain_graph(N_SITES), CHI0, seed=SEED)
@@ -219,13 +236,8 @@ def run_nsg(args):
     ctx.profile(False)
     launches = ctx.counters()["launches"] - launches0
     clk = clocks.stop()
-    t_sweep = float(np.sum(sweep_ms)) / 1e3
-    if dist:
-        import torch
-        tt = torch.tensor([t_sweep], device="cuda")
-        td.all_reduce(tt, op=td.ReduceOp.MAX)
-        t_sweep = float(tt.item())
-    value = world * args.steps / t_sweep
+    t_sweep = replica_time(float(np.sum(sweep_ms)) / 1e3, device="cuda" if dist else None)
+    value = replica_throughput(world, args.steps, t_sweep)
     # e2e: one sweep through the public API from host buffers (upload, sweep, download)
     e2e = None
     if rank == 0 and not args.no_e2e:

@@ -125,9 +125,13 @@ class SolvePool:
     in precision mode `precision`; `hbm_bytes` caps the summed footprints of the running
     jobs (default: 90 % of the device's free memory at start)."""
 
-    def __init__(self, workers=8, device=0, precision="fp64", hbm_bytes=None):
+    def __init__(self, workers=8, device=0, precision="fp64", hbm_bytes=None, context_factory=None, runner=None):
         self.workers, self.device, self.precision = int(workers), int(device), precision
         self.hbm_bytes = hbm_bytes
+        # context_factory() -> context with synchronize()/close(); runner(job, ctx) -> value.
+        # Defaults: a library context per worker and the DMRG / TDVP drivers.
+        self._make_ctx = context_factory or (lambda: _native.Context(self.device, precision=self.precision))
+        self._runner = runner or _run_job
 
     def run(self, jobs, time_scale=1.0):
         """Run `jobs` (arrival times in seconds, scaled by `time_scale`); returns the
@@ -169,8 +173,9 @@ class SolvePool:
                 lock.notify_all()
 
         def worker(wid):
-            ctx = _native.Context(self.device, precision=self.precision)
-            _native.set_thread_context(ctx)
+            ctx = self._make_ctx()
+            if isinstance(ctx, _native.Context):
+                _native.set_thread_context(ctx)
             try:
                 while True:
                     i = take()
@@ -180,7 +185,7 @@ class SolvePool:
                     start = time.perf_counter() - t0
                     err, val = None, None
                     try:
-                        val = _run_job(j, ctx)
+                        val = self._runner(j, ctx)
                         ctx.synchronize()
                     except Exception as e:  # reported per job, the pool keeps serving
                         err = f"{type(e).__name__}: {e}"
