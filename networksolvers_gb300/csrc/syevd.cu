@@ -1,7 +1,7 @@
 // Dense Hermitian eigensolver for the truncated factorizations:
 //   1. Householder reduction to a real symmetric tridiagonal T (one cooperative
 //      kernel, one grid barrier per column; the matrix stays L2-resident),
-//   2. Cuppen divide and conquer on T: Jacobi leaves of <= 32, rank-one merges with
+//   2. Cuppen divide and conquer on T: implicit-QL leaves of <= 32, rank-one merges with
 //      deflation (small z / close poles), secular roots by bracketed Newton with the
 //      origin at the nearer pole (one thread per root over many CTAs), Gu-Eisenstat
 //      recomputed z for orthogonal vectors, merged by an FP64 GEMM,
@@ -25,7 +25,6 @@
 
 namespace nsg {
 
-void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* w);  // eig.cu
 
 // Raise a kernel's dynamic shared-memory limit, never lower it.  The attribute is
 // process-wide and contexts on other host threads launch the same kernels concurrently
@@ -421,67 +420,121 @@ struct MergeDesc {
   double beta;
 };
 
-// Build dense leaf matrices (kLeaf x kLeaf, zero padded with distinct large diagonal
-// entries that are removed afterwards) from the modified tridiagonal.
-__global__ void leaf_build_kernel(const double* d, const double* e, const int* leaf_lo, const int* leaf_hi,
-                                  int nleaf, double* M) {
-  int L = blockIdx.x;
-  if (L >= nleaf) return;
-  int lo = leaf_lo[L], hi = leaf_hi[L], s = hi - lo;
-  double* A = M + (size_t)L * kLeaf * kLeaf;
-  for (int t = threadIdx.x; t < kLeaf * kLeaf; t += blockDim.x) {
-    int i = t % kLeaf, j = t / kLeaf;
-    double v = 0.0;
-    if (i < s && j < s) {
-      if (i == j)
-        v = d[lo + i];
-      else if (j == i + 1)
-        v = e[lo + i];
-      else if (i == j + 1)
-        v = e[lo + j];
+
+// Scatter leaf eigenpairs into Q (n x n, column-major) and w, sorted ascending.
+// Leaves of the divide and conquer: the symmetric tridiagonal blocks (order <= 32) are
+// diagonalised by the implicit QL method with Wilkinson shifts (Givens chase from the
+// bottom of the unreduced block to its top), one warp per leaf.  Lane 0 runs each
+// chase's scalar recurrence and records its rotations; then every lane applies them, in
+// order, to its own row of the eigenvector matrix Z (columns = eigenvectors).  The
+// eigenpairs are sorted ascending and written into the leaf's diagonal block of Q and w.
+// A block that fails to converge in 60 chases per eigenvalue raises *err.
+constexpr int kLeafWarps = 4;
+__global__ void __launch_bounds__(32 * kLeafWarps)
+    leaf_ql_kernel(const double* __restrict__ dsrc, const double* __restrict__ esrc, const int* leaf_lo,
+                   const int* leaf_hi, int nleaf, double* Q, int n, double* w, int* err) {
+  __shared__ double Zs[kLeafWarps][kLeaf][kLeaf + 1];
+  __shared__ double ds_[kLeafWarps][kLeaf], es_[kLeafWarps][kLeaf], cs_[kLeafWarps][kLeaf],
+      sn_[kLeafWarps][kLeaf];
+  __shared__ int ord_[kLeafWarps][kLeaf];
+  const int wl = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int L = blockIdx.x * kLeafWarps + wl;
+  if (L >= nleaf) return;  // whole warps only
+  const int lo = leaf_lo[L], s = leaf_hi[L] - lo;
+  double(*Z)[kLeaf + 1] = Zs[wl];
+  double* d = ds_[wl];
+  double* e = es_[wl];
+  for (int c = 0; c < kLeaf; ++c) Z[lane][c] = (lane == c) ? 1.0 : 0.0;
+  if (lane < s) {
+    d[lane] = dsrc[lo + lane];
+    e[lane] = (lane + 1 < s) ? esrc[lo + lane] : 0.0;
+  }
+  __syncwarp();
+  const double eps = 2.220446049250313e-16;
+  bool failed = false;
+  for (int l = 0; l < s && !failed; ++l) {
+    for (int iter = 0;; ++iter) {
+      int m = l;
+      while (m < s - 1) {
+        const double dd = fabs(d[m]) + fabs(d[m + 1]);
+        if (fabs(e[m]) <= eps * dd) break;
+        ++m;
+      }
+      if (m == l) break;
+      if (iter == 60) {
+        failed = true;
+        break;
+      }
+      int lowest = l;  // rotations recorded for i = m-1 .. lowest
+      if (lane == 0) {
+        double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+        double r = sqrt(g * g + 1.0);
+        g = d[m] - d[l] + e[l] / (g + (g >= 0.0 ? r : -r));
+        double sv = 1.0, cv = 1.0, p = 0.0;
+        int i = m - 1;
+        for (; i >= l; --i) {
+          const double f = sv * e[i], b = cv * e[i];
+          r = sqrt(f * f + g * g);
+          e[i + 1] = r;
+          if (r == 0.0) {  // the block splits: undo the pending shift and restart
+            d[i + 1] -= p;
+            e[m] = 0.0;
+            break;
+          }
+          const double ir = 1.0 / r;
+          sv = f * ir;
+          cv = g * ir;
+          g = d[i + 1] - p;
+          r = (d[i] - g) * sv + 2.0 * cv * b;
+          p = sv * r;
+          d[i + 1] = g + p;
+          g = cv * r - b;
+          cs_[wl][i] = cv;
+          sn_[wl][i] = sv;
+        }
+        if (i < l) {
+          d[l] -= p;
+          e[l] = g;
+          e[m] = 0.0;
+        } else {
+          lowest = i + 1;
+        }
+        ord_[wl][0] = lowest;
+      }
+      __syncwarp();
+      lowest = ord_[wl][0];
+      // each lane rotates its row of Z through the chase's rotations, in order
+      for (int i = m - 1; i >= lowest; --i) {
+        const double cv = cs_[wl][i], sv = sn_[wl][i];
+        const double f = Z[lane][i + 1], zi = Z[lane][i];
+        Z[lane][i + 1] = sv * zi + cv * f;
+        Z[lane][i] = cv * zi - sv * f;
+      }
+      __syncwarp();
     }
-    A[t] = v;
+  }
+  if (failed && lane == 0) atomicExch(err, 1);
+  // ascending order (insertion sort by lane 0), then the leaf's block of Q and w
+  if (lane == 0) {
+    int* o = ord_[wl];
+    for (int a = 0; a < s; ++a) o[a] = a;
+    for (int a = 1; a < s; ++a) {
+      const int x = o[a];
+      int b2 = a - 1;
+      while (b2 >= 0 && d[o[b2]] > d[x]) {
+        o[b2 + 1] = o[b2];
+        --b2;
+      }
+      o[b2 + 1] = x;
+    }
+  }
+  __syncwarp();
+  if (lane < s) {
+    for (int j = 0; j < s; ++j) Q[(size_t)(lo + j) * n + (lo + lane)] = Z[lane][ord_[wl][j]];
+    w[lo + lane] = d[ord_[wl][lane]];
   }
 }
 
-// Scatter leaf eigenpairs into Q (n x n, column-major) and w, sorted ascending.
-__global__ void leaf_scatter_kernel(const double* M, const double* V, const double* wl, const int* leaf_lo,
-                                    const int* leaf_hi, int nleaf, double* Q, int n, double* w) {
-  int L = blockIdx.x;
-  if (L >= nleaf) return;
-  int lo = leaf_lo[L], hi = leaf_hi[L], s = hi - lo;
-  const double* Vl = V + (size_t)L * kLeaf * kLeaf;
-  const double* wv = wl + (size_t)L * kLeaf;
-  __shared__ int order[kLeaf];
-  if (threadIdx.x == 0) {
-    // eigenpairs that belong to the leaf: the padding rows/cols are zero, so the
-    // padded eigenvectors are unit vectors on indices >= s; pick vectors with support < s
-    int cnt = 0;
-    int idx[kLeaf];
-    for (int j = 0; j < kLeaf; ++j) {
-      double tail = 0.0;
-      for (int i = s; i < kLeaf; ++i) tail += fabs(Vl[i + j * kLeaf]);
-      if (tail < 0.5 && cnt < s) idx[cnt++] = j;
-    }
-    // insertion sort by eigenvalue
-    for (int a = 1; a < cnt; ++a) {
-      int x = idx[a];
-      int b = a - 1;
-      while (b >= 0 && wv[idx[b]] > wv[x]) {
-        idx[b + 1] = idx[b];
-        --b;
-      }
-      idx[b + 1] = x;
-    }
-    for (int a = 0; a < s; ++a) order[a] = a < cnt ? idx[a] : 0;
-  }
-  __syncthreads();
-  for (int t = threadIdx.x; t < s * s; t += blockDim.x) {
-    int i = t % s, j = t / s;
-    Q[(size_t)(lo + j) * n + (lo + i)] = Vl[i + order[j] * kLeaf];
-  }
-  for (int j = threadIdx.x; j < s; j += blockDim.x) w[lo + j] = wv[order[j]];
-}
 
 // Per merge (one CTA, serial parts on thread 0): gather D and z, flip for rho < 0,
 // sort, normalise z, deflate.  Outputs (per merge, arrays of length nb = hi - lo, at
@@ -1165,16 +1218,16 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
   DevBuf dlo(c, sizeof(int) * nleaf), dhi(c, sizeof(int) * nleaf);
   NSG_CUDA(cudaMemcpyAsync(dlo.p, llo.data(), sizeof(int) * nleaf, cudaMemcpyHostToDevice, c->stream));
   NSG_CUDA(cudaMemcpyAsync(dhi.p, lhi.data(), sizeof(int) * nleaf, cudaMemcpyHostToDevice, c->stream));
-  DevBuf LM(c, sizeof(double) * nleaf * kLeaf * kLeaf), LV(c, sizeof(double) * nleaf * kLeaf * kLeaf),
-      LW(c, sizeof(double) * nleaf * kLeaf);
-  leaf_build_kernel<<<nleaf, 256, 0, c->stream>>>(dd.as<double>(), de.as<double>(), dlo.as<int>(), dhi.as<int>(),
-                                                  nleaf, LM.as<double>());
-  count_launch(c);
-  jacobi_batched(c, kLeaf, nleaf, LM.as<double>(), LV.as<double>(), LW.as<double>());
-  leaf_scatter_kernel<<<nleaf, 256, 0, c->stream>>>(LM.as<double>(), LV.as<double>(), LW.as<double>(), dlo.as<int>(),
-                                                    dhi.as<int>(), nleaf, Q, n, w);
+  DevBuf lerr(c, sizeof(int));
+  NSG_CUDA(cudaMemsetAsync(lerr.p, 0, sizeof(int), c->stream));
+  leaf_ql_kernel<<<(nleaf + kLeafWarps - 1) / kLeafWarps, 32 * kLeafWarps, 0, c->stream>>>(
+      dd.as<double>(), de.as<double>(), dlo.as<int>(), dhi.as<int>(), nleaf, Q, n, w, lerr.as<int>());
   count_launch(c);
   check_launch("dc leaves");
+  int leaf_failed = 0;
+  NSG_CUDA(cudaMemcpyAsync(&leaf_failed, lerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  NSG_CHECK(leaf_failed == 0, NSG_ERR_NONFINITE, "eigensolver: a tridiagonal leaf did not converge");
   // merges, deepest level first
   MergeWork W;
   DevBuf bDs(c, sizeof(double) * n), bzs(c, sizeof(double) * n), bperm(c, sizeof(int) * n), bkind(c, sizeof(int) * n),
