@@ -284,9 +284,12 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
   int64_t ksplit = g.K;
   const int64_t tiles = gx * gy * g.batch;
   const int64_t sms = c->num_sms > 0 ? c->num_sms : 152;
-  if (tiles < sms && g.K >= 512) {
+  if (tiles < sms && g.K >= 64) {
+    // small outputs (the eigensolver's GEMMs at bond dimension <= 128 have a handful of
+    // tiles): spread K over more SMs, down to 32-deep slices; the FP64 pipe of one SM is
+    // the bound otherwise
     int64_t want = (2 * sms + tiles - 1) / tiles;
-    int64_t maxs = g.K / 256;
+    int64_t maxs = g.K >= 512 ? g.K / 256 : g.K / 32;
     splits = int(std::min<int64_t>({want, maxs, 64}));
     if (splits < 2) splits = 1;
     ksplit = (g.K + splits - 1) / splits;
