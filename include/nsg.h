@@ -176,6 +176,19 @@ int nsg_eigh(nsg_ctx* ctx, const nsg_tensor* rho, const int* row_axes, int n_row
              double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
              double* evals, int64_t evals_cap, int64_t* newdim, double* truncerr);
 
+/* ---- fused region step ----------------------------------------------------
+ * One two-site DMRG region step on a chain in one call (the extracter product,
+ * extracter.jl:7; the Lanczos updater, eigsolve.jl:14-28; the truncated-factorization
+ * inserter, inserter.jl:3-33), composed of the entry points above:
+ *   L [a', wl, a], W1 [wl, s1', s1, wm], W2 [wm, s2', s2, wr], R [b', wr, b] (the fixed
+ *   tensors of optimal_map, operator_map.jl:3-10), psi1 [a, s1, c], psi2 [c, s2, b].
+ * Outputs U [a, s1, k] (new psi1, left-orthonormal), C [k, s2, b] (new psi2), the
+ * Lanczos eigenvalue, the new bond dimension k and the relative discarded weight. */
+int nsg_region_step(nsg_ctx* ctx, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, nsg_tensor* R,
+                    const nsg_tensor* psi1, const nsg_tensor* psi2, int krylovdim, int maxiter,
+                    double tol, double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
+                    nsg_tensor** C, double* energy, int64_t* newdim, double* truncerr);
+
 /* ---- allocation-free GEMM -------------------------------------------------
  * No counterpart in the reference: an addition for callers that must not allocate
  * device memory themselves (a Julia program whose CUDA.jl memory pool owns the device,

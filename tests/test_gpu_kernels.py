@@ -312,3 +312,38 @@ def test_eigensolver_large_and_degenerate(nsg_ctx, cplx, m, n, precision):
         Pk = u @ Cc.to_numpy().reshape(kref, n)
         assert abs(np.linalg.norm(M - Pk) ** 2 / np.linalg.norm(M) ** 2 - errref) < 1e-12
         assert rel(info["spectrum"][:kref], s[:kref] ** 2) < 1e-12
+
+
+def test_fused_region_step_matches_call_by_call(nsg_ctx):
+    """nsg_region_step (product, Lanczos, truncated factorization in one call) against
+    the same region step taken entry point by entry point."""
+    import networksolvers_gb300.models as models
+    from networksolvers_gb300.kernelbench import _FixedMap
+    from networksolvers_gb300.network import LinearMap
+    from networksolvers_gb300.sweep import eigsolve_solver, region_step
+    rng = np.random.default_rng(11)
+    chi, d = 40, 2
+    W = models.heisenberg_chain(4).tensors[2]
+    w = W.shape[0]
+    a, b, cc, s1, s2 = Index(chi), Index(chi), Index(chi), Index(d), Index(d)
+    w1, w2, w3 = Index(w), Index(w), Index(w)
+    Ln = rng.standard_normal((chi, w, chi))
+    Rn = rng.standard_normal((chi, w, chi))
+    L = DTensor.from_numpy(Ln + Ln.transpose(2, 1, 0), [a.prime(), w1, a])
+    R = DTensor.from_numpy(Rn + Rn.transpose(2, 1, 0), [b.prime(), w3, b])
+    W1 = DTensor.from_numpy(W, [w1, s1.prime(), s1, w2])
+    W2 = DTensor.from_numpy(W, [w2, s2.prime(), s2, w3])
+    p1 = DTensor.from_numpy(rng.standard_normal((chi, d, chi)), [a, s1, cc])
+    p2 = DTensor.from_numpy(rng.standard_normal((chi, d, chi)), [cc, s2, b])
+    E1, U1, C1, info1 = region_step(L, W1, W2, R, p1, p2, krylovdim=3, maxiter=1, cutoff=1e-10, maxdim=30)
+    local = contract([p1, p2], out=[a, s1, s2, b])
+    lm = LinearMap(_FixedMap([L, R, W1, W2]), [a, s1, s2, b])
+    E2, x = eigsolve_solver(lm, local, krylovdim=3, maxiter=1)
+    U2, C2, info2 = it.factorize(x, [a, s1], cutoff=1e-10, maxdim=30)
+    assert abs(E1 - E2) <= 1e-13 * abs(E2)
+    assert info1["newdim"] == info2["newdim"] == 30
+    assert abs(info1["truncerr"] - info2["truncerr"]) <= 1e-14
+    k = info1["newdim"]
+    P1 = U1.to_numpy().reshape(chi * d, k) @ C1.to_numpy().reshape(k, d * chi)
+    P2 = U2.to_numpy().reshape(chi * d, k) @ C2.to_numpy().reshape(k, d * chi)
+    assert rel(P1, P2) < 1e-12
