@@ -3,14 +3,12 @@
 //   qr(...)                                               extracter.jl:6, applyexp.jl:37
 //   eigen(rho; trunc..., ishermitian=true)                 subspace/densitymatrix.jl:53
 //
-// The SVD of the matricised tensor M (m x n) goes through the Hermitian Gram matrix
-// G = M M^H: G = Z diag(lambda) Z^H gives the left singular vectors U = Z and
+// The SVD of the matricised tensor M (m x n) goes through a Hermitian Gram matrix.
+// m <= n: G = M M^H = Z diag(lambda) Z^H gives the left singular vectors U = Z and
 // sigma^2 = lambda, and C = U^H M = S V^H is the right factor that `factorize` with
-// ortho="left" stores (U -> psi[v1], C -> psi[v2]).  The eigensolver is a parallel
-// cyclic Jacobi method (round-robin pairing, n/2 disjoint rotations per round,
-// complex Hermitian rotations for complex128).  Its orthogonality is at the unit
-// roundoff regardless of eigenvalue clustering, which the spectra of DMRG bonds
-// (exact SU(2) multiplets, long tails) need.
+// ortho="left" stores (U -> psi[v1], C -> psi[v2]).  m > n: the narrow side's Gram
+// matrix M^H M = V S^2 V^H, U = M V S^-1 re-orthogonalised, C = U^H M.  The Hermitian
+// eigenproblems go to the tridiagonalisation + divide-and-conquer solver (syevd.cu).
 //
 // Truncation rule (NDTensors, restated): spectrum P = lambda sorted descending,
 // negative tail zeroed; cut to maxdim; then drop from the end while
@@ -24,179 +22,6 @@
 namespace nsg {
 
 namespace {
-
-constexpr int kJacobiThreads = 1024;
-constexpr int kJacobiMaxN = 2048;
-
-__device__ __forceinline__ double re_(double v) { return v; }
-__device__ __forceinline__ double re_(double2 v) { return v.x; }
-__device__ __forceinline__ double abs_(double v) { return fabs(v); }
-__device__ __forceinline__ double abs_(double2 v) { return hypot(v.x, v.y); }
-
-// rotate a pair (x_p, x_q) with J = [[c, s], [-s e, c e]] where e = conj(phase) (columns)
-// For real data phase = 1.
-__device__ __forceinline__ void rot_cols(double& xp, double& xq, double c, double s, double2 e) {
-  // real case: e = sign(G_pq)
-  double a = xp, b = e.x * xq;
-  xp = c * a - s * b;
-  xq = s * a + c * b;
-}
-__device__ __forceinline__ void rot_cols(double2& xp, double2& xq, double c, double s, double2 e) {
-  // col_p' = c col_p - s e col_q ; col_q' = s col_p + c e col_q   with e = exp(-i phi)
-  double2 a = xp, b = xq;
-  double2 eb = make_double2(e.x * b.x - e.y * b.y, e.x * b.y + e.y * b.x);
-  xp = make_double2(c * a.x - s * eb.x, c * a.y - s * eb.y);
-  xq = make_double2(s * a.x + c * eb.x, s * a.y + c * eb.y);
-}
-__device__ __forceinline__ void rot_rows(double& xp, double& xq, double c, double s, double2 e) {
-  double a = xp, b = e.x * xq;
-  xp = c * a - s * b;
-  xq = s * a + c * b;
-}
-__device__ __forceinline__ void rot_rows(double2& xp, double2& xq, double c, double s, double2 e) {
-  // rows <- J^H rows: row_p' = c row_p - s conj(e) row_q ; row_q' = s row_p + c conj(e) row_q
-  double2 a = xp, b = xq;
-  double2 ce = make_double2(e.x, -e.y);
-  double2 eb = make_double2(ce.x * b.x - ce.y * b.y, ce.x * b.y + ce.y * b.x);
-  xp = make_double2(c * a.x - s * eb.x, c * a.y - s * eb.y);
-  xq = make_double2(s * a.x + c * eb.x, s * a.y + c * eb.y);
-}
-__device__ __forceinline__ double2 phase_of(double b) { return make_double2(b >= 0 ? 1.0 : -1.0, 0.0); }
-__device__ __forceinline__ double2 phase_of(double2 b) {
-  double r = hypot(b.x, b.y);
-  return r > 0 ? make_double2(b.x / r, -b.y / r) : make_double2(1.0, 0.0);  // exp(-i phi)
-}
-__device__ __forceinline__ void set_one(double& v) { v = 1.0; }
-__device__ __forceinline__ void set_one(double2& v) { v = make_double2(1.0, 0.0); }
-__device__ __forceinline__ void set_zero(double& v) { v = 0.0; }
-__device__ __forceinline__ void set_zero(double2& v) { v = make_double2(0.0, 0.0); }
-
-// One CTA diagonalises G (n x n, column-major, Hermitian, overwritten) and writes V.
-// Round-robin schedule over N = n rounded up to even players: in round r, player N-1
-// meets r, and (r+i) mod (N-1) meets (r-i) mod (N-1) for i = 1..N/2-1.
-template <typename T>
-__global__ void __launch_bounds__(kJacobiThreads)
-    jacobi_kernel(T* __restrict__ G, int n, T* __restrict__ V, double* __restrict__ w, int max_sweeps,
-                  int* __restrict__ sweeps_out) {
-  // batched: CTA b works on matrix b (consecutive n x n blocks)
-  G += (size_t)blockIdx.x * n * n;
-  V += (size_t)blockIdx.x * n * n;
-  w += (size_t)blockIdx.x * n;
-  __shared__ double cs_[kJacobiMaxN / 2], sn_[kJacobiMaxN / 2];
-  __shared__ double2 ph_[kJacobiMaxN / 2];
-  __shared__ int p_[kJacobiMaxN / 2], q_[kJacobiMaxN / 2];
-  __shared__ int any_rot;
-  __shared__ double red[kJacobiThreads / 32];
-  __shared__ double scale;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  const int64_t nn = int64_t(n) * n;
-  for (int64_t e = tid; e < nn; e += nt) {
-    int64_t i = e % n, j = e / n;
-    if (i == j)
-      set_one(V[e]);
-    else
-      set_zero(V[e]);
-  }
-  // Frobenius norm of G for the absolute threshold
-  double loc = 0.0;
-  for (int64_t e = tid; e < nn; e += nt) {
-    double a = abs_(G[e]);
-    loc += a * a;
-  }
-  for (int o = 16; o > 0; o >>= 1) loc += __shfl_down_sync(0xffffffffu, loc, o);
-  if ((tid & 31) == 0) red[tid >> 5] = loc;
-  __syncthreads();
-  if (tid == 0) {
-    double s = 0;
-    for (int k = 0; k < (nt + 31) / 32; ++k) s += red[k];
-    scale = sqrt(s);
-  }
-  __syncthreads();
-  const double abs_thr = 1e-17 * scale;
-  const int N = n + (n & 1);
-  const int npairs = N / 2;
-  int sweep = 0;
-  for (; sweep < max_sweeps; ++sweep) {
-    if (tid == 0) any_rot = 0;
-    __syncthreads();
-    for (int r = 0; r < N - 1; ++r) {
-      for (int k = tid; k < npairs; k += nt) {
-        int p, q;
-        if (k == 0) {
-          p = N - 1;
-          q = r;
-        } else {
-          p = (r + k) % (N - 1);
-          q = (r - k + (N - 1)) % (N - 1);
-        }
-        if (p > q) {
-          int t = p;
-          p = q;
-          q = t;
-        }
-        double c = 1.0, s = 0.0;
-        double2 e = make_double2(1.0, 0.0);
-        if (q < n) {
-          double a = re_(G[p + int64_t(n) * p]), d = re_(G[q + int64_t(n) * q]);
-          T b = G[p + int64_t(n) * q];
-          double bb = abs_(b);
-          if (bb > abs_thr && bb > 1e-16 * sqrt(fabs(a) * fabs(d))) {
-            double theta = (d - a) / (2.0 * bb);
-            double t = (theta >= 0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            c = 1.0 / sqrt(t * t + 1.0);
-            s = t * c;
-            e = phase_of(b);
-            any_rot = 1;
-          }
-        }
-        p_[k] = p;
-        q_[k] = (q < n) ? q : -1;
-        cs_[k] = c;
-        sn_[k] = s;
-        ph_[k] = e;
-      }
-      __syncthreads();
-      // columns of G and V
-      const int64_t tasks = int64_t(npairs) * n;
-      for (int64_t t = tid; t < tasks; t += nt) {
-        int k = int(t / n), i = int(t % n);
-        int q = q_[k];
-        if (q < 0 || sn_[k] == 0.0) continue;
-        int p = p_[k];
-        rot_cols(G[i + int64_t(n) * p], G[i + int64_t(n) * q], cs_[k], sn_[k], ph_[k]);
-        rot_cols(V[i + int64_t(n) * p], V[i + int64_t(n) * q], cs_[k], sn_[k], ph_[k]);
-      }
-      __syncthreads();
-      // rows of G
-      for (int64_t t = tid; t < tasks; t += nt) {
-        int k = int(t / n), j = int(t % n);
-        int q = q_[k];
-        if (q < 0 || sn_[k] == 0.0) continue;
-        int p = p_[k];
-        rot_rows(G[p + int64_t(n) * j], G[q + int64_t(n) * j], cs_[k], sn_[k], ph_[k]);
-      }
-      __syncthreads();
-    }
-    if (!any_rot) break;
-    __syncthreads();
-  }
-  for (int i = tid; i < n; i += nt) w[i] = re_(G[i + int64_t(n) * i]);
-  if (tid == 0 && sweeps_out) sweeps_out[blockIdx.x] = sweep;
-}
-
-struct Spectrum {
-  std::vector<int> order;  // indices sorted by descending eigenvalue
-  std::vector<double> P;   // sorted, negative tail zeroed
-};
-
-Spectrum sorted_spectrum(const std::vector<double>& w) {
-  Spectrum s;
-  s.order.resize(w.size());
-  std::iota(s.order.begin(), s.order.end(), 0);
-  std::stable_sort(s.order.begin(), s.order.end(), [&](int a, int b) { return w[a] > w[b]; });
-  for (int i : s.order) s.P.push_back(w[i]);
-  return s;
-}
 
 // NDTensors truncation rule; returns kept count and relative discarded weight.
 int64_t truncate_rule(std::vector<double> P, int64_t origm, double cutoff, int64_t maxdim, int64_t mindim,
@@ -299,26 +124,6 @@ __global__ void half_newton_kernel(T* G, int64_t k) {
 }
 
 }  // namespace
-
-void jacobi_batched(nsg_ctx* c, int n, int batch, double* A, double* V, double* w) {
-  NSG_CHECK(n >= 1 && n <= kJacobiMaxN && batch >= 1, NSG_ERR_INVALID, "jacobi_batched: bad size");
-  int threads = n <= 64 ? 128 : kJacobiThreads;
-  jacobi_kernel<double><<<batch, threads, 0, c->stream>>>(A, n, V, w, 60, nullptr);
-  count_launch(c);
-  check_launch("jacobi_batched");
-}
-
-void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev) {
-  NSG_CHECK(n >= 1 && n <= kJacobiMaxN, NSG_ERR_UNSUPPORTED,
-            "eigensolver: matrix order " + std::to_string(n) + " above the supported maximum");
-  int threads = kJacobiThreads;
-  if (dtype == NSG_C128)
-    jacobi_kernel<double2><<<1, threads, 0, c->stream>>>((double2*)A, int(n), (double2*)V, w_dev, 60, nullptr);
-  else
-    jacobi_kernel<double><<<1, threads, 0, c->stream>>>((double*)A, int(n), (double*)V, w_dev, 60, nullptr);
-  count_launch(c);
-  check_launch("jacobi");
-}
 
 }  // namespace nsg
 

@@ -153,9 +153,6 @@ void copy_rows(nsg_ctx* c, int dtype, int64_t nrows_out, int64_t ncols, const vo
                int64_t lds, void* dst, int64_t ldd);
 void row_norms2(nsg_ctx* c, int dtype, int64_t rows, int64_t cols, const void* A, int64_t lda,
                 double* out_dev);
-// symmetric/Hermitian eigen of a dense n x n matrix (column-major, overwritten);
-// eigenvectors to V (n x n), eigenvalues (unsorted) to w_dev.
-void syevd(nsg_ctx* c, int dtype, int64_t n, void* A, void* V, double* w_dev);
 
 // Hermitian eigensolver (tridiagonalisation + divide and conquer + back-transformation).
 // A (n x n) is consumed.  `pick` receives the eigenvalues in ascending order and returns
