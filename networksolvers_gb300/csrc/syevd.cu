@@ -1180,15 +1180,15 @@ struct DevBuf {
 };
 
 static void build_tree(int lo, int hi, std::vector<std::vector<MergeDesc>>& levels, std::vector<int>& leaf_lo,
-                       std::vector<int>& leaf_hi, int depth) {
-  if (hi - lo <= kLeaf) {
+                       std::vector<int>& leaf_hi, int depth, int leaf) {
+  if (hi - lo <= leaf) {
     leaf_lo.push_back(lo);
     leaf_hi.push_back(hi);
     return;
   }
   int mid = lo + (hi - lo) / 2;
-  build_tree(lo, mid, levels, leaf_lo, leaf_hi, depth + 1);
-  build_tree(mid, hi, levels, leaf_lo, leaf_hi, depth + 1);
+  build_tree(lo, mid, levels, leaf_lo, leaf_hi, depth + 1, leaf);
+  build_tree(mid, hi, levels, leaf_lo, leaf_hi, depth + 1, leaf);
   if ((int)levels.size() <= depth) levels.resize(depth + 1);
   levels[depth].push_back(MergeDesc{lo, mid, hi, 0.0});
 }
@@ -1199,7 +1199,10 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
                        double* w) {
   std::vector<std::vector<MergeDesc>> levels;
   std::vector<int> llo, lhi;
-  build_tree(0, n, levels, llo, lhi, 0);
+  // leaves of 16 up to order 256 (the QL leaves are latency bound: FP64 chains), of 32
+  // above (each extra merge level costs a batch of launches); measured on GB300
+  const int leaf = n <= 256 ? 16 : kLeaf;
+  build_tree(0, n, levels, llo, lhi, 0, leaf);
   // modified diagonal: for each split subtract beta at the two touching diagonals
   std::vector<double> d = d_in;
   for (auto& lv : levels)
