@@ -8,9 +8,12 @@ One step = one full sweep (198 two-site regions).  Warm-up steps are the first W
 of the schedule, the timed steps the next K sweeps.  Metric: sweeps/s (higher is
 better); the split-precision form is the product path: the large contractions (H_eff,
 environments) run as six-slice BF16 products with exact FP32 chunk accumulation on
-tcgen05 (FP64-level results), while the Gram matrix, eigensolver and Lanczos scalars
-stay FP64; `--precision tf32x3` is the three-product TF32 form and `--precision fp64`
-the plain form (every contraction on the FP64 CUDA cores).
+tcgen05, the eigensolver's GEMMs, `C = U^H M` and the density-matrix expansion as
+eight-slice products (FP64 accuracy), while the Gram matrices, the tridiagonalisation,
+the secular equations and the Lanczos scalars stay FP64; `--precision tf32x3` is the
+three-product TF32 form and `--precision fp64` the plain form (every contraction on the
+FP64 CUDA cores).  Other workloads (`--workload c1|tdvp|batch|serve|accuracy`) print
+their own lines; see `main()`.
 
 Timing: CUDA events on the library's stream around each timed sweep; the per-kernel
 roofline comes from events around each launch of the dominant kernel classes in the
