@@ -304,6 +304,107 @@ def chain_operator(n, J1=1.0, J2=0.0, delta=1.0, h=None):
     return Network(g, tensors, legs, np.float64, {"kind": "operator", "w": w})
 
 
+# ----------------------------------------------------------------------------
+# OpSum -> chain MPO (the input format of the reference's tests and examples: itn.mpo /
+# itn.ttn of an OpSum, e.g. test_tree_dmrg.jl:28)
+# ----------------------------------------------------------------------------
+
+SITE_OPS = {"Sz": SZ, "S+": SP, "S-": SM, "Sx": 0.5 * PX, "Id": ID2, "X": PX, "Z": PZ,
+            "Sy": np.array([[0.0, -0.5j], [0.5j, 0.0]]), "Y": np.array([[0.0, -1.0j], [1.0j, 0.0]]),
+            "N": np.array([[0.0, 0.0], [0.0, 1.0]])}
+
+
+class OpSum:
+    """A sum of products of on-site operators, written as in ITensors:
+    `os.add(coef, "Sz", i, "Sz", j)` or `os += (coef, "S+", i, "S-", j)`.  Operators are
+    names of SITE_OPS (S=1/2 basis order Up, Dn) or d x d arrays; sites are 1-based."""
+
+    def __init__(self):
+        self.terms = []
+
+    def add(self, coef, *ops):
+        if len(ops) % 2 or not ops:
+            raise ValueError("OpSum.add(coef, op1, site1, op2, site2, ...)")
+        factors = []
+        for k in range(0, len(ops), 2):
+            op, site = ops[k], int(ops[k + 1])
+            mat = SITE_OPS[op] if isinstance(op, str) else np.asarray(op)
+            factors.append((site, mat))
+        self.terms.append((coef, factors))
+        return self
+
+    def __iadd__(self, term):
+        return self.add(*term)
+
+
+def chain_mpo(opsum, n, d=2):
+    """Exact MPO of an OpSum on a chain of n sites by the finite-state construction: on
+    the bond (j, j+1) the automaton is in START (no operator placed), DONE (all placed) or
+    in the private state of one term whose first site is <= j and last site > j, so the
+    bond dimension is 2 + the number of terms spanning it (5 for the Heisenberg chain).
+    Operators of one term on the same site multiply in the order given."""
+    g = chain_graph(n)
+    cplx = any(np.iscomplexobj(m) or np.iscomplexobj(c) for c, fs in opsum.terms for _, m in fs)
+    dt = np.complex128 if cplx else np.float64
+    START, DONE = 0, 1
+    terms = []
+    for c, fs in opsum.terms:
+        per = {}
+        for site, mat in fs:
+            if not 1 <= site <= n:
+                raise ValueError(f"OpSum site {site} outside 1..{n}")
+            per[site] = per[site] @ mat if site in per else np.asarray(mat, dtype=dt)
+        sites = sorted(per)
+        terms.append((c, per, sites[0], sites[-1]))
+    # bond states: bond b between sites b and b+1 (b = 1..n-1)
+    state = {}
+    bdim = {}
+    for b in range(1, n):
+        k = 2
+        for t, (_, _, f, l) in enumerate(terms):
+            if f <= b < l:
+                state[(t, b)] = k
+                k += 1
+        bdim[b] = k
+    ident = np.eye(d, dtype=dt)
+    tensors, legs = {}, {}
+    for j in range(1, n + 1):
+        wl = bdim.get(j - 1, 1)
+        wr = bdim.get(j, 1)
+        W = np.zeros((wl, d, d, wr), dtype=dt)   # [left, s', s, right]
+        lstart = 0 if j > 1 else 0
+        rdone = 1 if j < n else 0
+        if j > 1:
+            W[DONE, :, :, rdone] += ident
+        if j < n:
+            W[lstart, :, :, START] += ident
+        for t, (c, per, f, l) in enumerate(terms):
+            op = per.get(j, ident)
+            if f == l == j:
+                W[lstart, :, :, rdone] += c * op
+            elif f == j:
+                W[lstart, :, :, state[(t, j)]] += c * op
+            elif f < j < l:
+                W[state[(t, j - 1)], :, :, state[(t, j)]] += op
+            elif j == l and f < j:
+                W[state[(t, j - 1)], :, :, rdone] += op
+        el = g.edge_key(j - 1, j) if j > 1 else None
+        er = g.edge_key(j, j + 1) if j < n else None
+        if n == 1:
+            tensors[j] = W[0, :, :, 0].copy()
+            legs[j] = [('sp', j), ('s', j)]
+        elif j == 1:
+            tensors[j] = np.ascontiguousarray(W[0].transpose(2, 0, 1))   # [right, s', s]
+            legs[j] = [('w', er), ('sp', j), ('s', j)]
+        elif j == n:
+            tensors[j] = np.ascontiguousarray(W[:, :, :, 0])            # [left, s', s]
+            legs[j] = [('w', el), ('sp', j), ('s', j)]
+        else:
+            tensors[j] = np.ascontiguousarray(W)
+            legs[j] = [('w', el), ('sp', j), ('s', j), ('w', er)]
+    return Network(g, tensors, legs, dt, {"kind": "operator", "w": max(bdim.values()) if bdim else 1})
+
+
 def heisenberg_chain(n, J=1.0):
     return chain_operator(n, J1=J, J2=0.0, delta=1.0)
 

@@ -193,3 +193,30 @@ def test_split_form_tracks_plain_form_region_by_region(nsg_ctx):
     assert np.array_equal(rs[:, 3], rp[:, 3])
     assert np.max(np.abs(rs[:, 2] - rp[:, 2]) / np.abs(rp[:, 2])) < 1e-10
     assert abs(Es - Ep) / abs(Ep) < 1e-10
+
+
+def test_opsum_hamiltonian_dmrg_matches_oracle(nsg_ctx):
+    """A Hamiltonian written as an OpSum (next-nearest-neighbour exchange, a transverse
+    field, a three-site term) compiled to a chain MPO, through the GPU drivers and the
+    oracle: per-region energies 1e-10 relative and identical bond dimensions."""
+    from oracle import sweep as osw
+    n = 12
+    os_ = m.OpSum()
+    for j in range(1, n):
+        os_ += (1.0, "Sz", j, "Sz", j + 1)
+        os_ += (0.5, "S+", j, "S-", j + 1)
+        os_ += (0.5, "S-", j, "S+", j + 1)
+    for j in range(1, n - 1):
+        os_ += (0.25, "Sz", j, "Sz", j + 2)
+        os_ += (0.1, "Sx", j, "Sz", j + 1, "Sx", j + 2)
+    for j in range(1, n + 1):
+        os_ += (0.3, "Sx", j)
+    H = m.chain_mpo(os_, n)
+    psi0 = m.random_state(m.chain_graph(n), 8, seed=2)
+    kw = dict(nsweeps=3, nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+              inserter_kwargs=dict(trunc=dict(cutoff=1e-10, maxdim=32)))
+    E, r, _ = _record_dmrg(ns.dmrg, H, psi0, **kw)
+    Eo, ro, _ = _record_dmrg(osw.dmrg, H, psi0, **kw)
+    assert np.array_equal(r[:, 3], ro[:, 3])
+    assert np.max(np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])) < 1e-10
+    assert abs(E - Eo) / abs(Eo) < 1e-10
