@@ -220,3 +220,39 @@ def test_opsum_hamiltonian_dmrg_matches_oracle(nsg_ctx):
     assert np.array_equal(r[:, 3], ro[:, 3])
     assert np.max(np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])) < 1e-10
     assert abs(E - Eo) / abs(Eo) < 1e-10
+
+
+@pytest.mark.parametrize("nsites", [1, 2])
+def test_tree_dmrg_with_jumping_post_order_plan(nsg_ctx, nsites):
+    """Environment-cache bookkeeping on a tree when consecutive regions are not adjacent:
+    DMRG sweeps that follow the post-order DFS plan (dfs_plans.jl:5-16; each move to the
+    next region is a gauge walk over several edges and invalidates the environments on
+    the way) on the GPU and in the oracle — per-region energies 1e-10 and bond dimensions
+    equal."""
+    from oracle import network as on, sweep as osw
+    g = m.build_tree_graph(3, 2)
+    H = m.heisenberg_tree(g)
+    psi0 = m.random_state(g, 4, seed=5)
+    trunc = dict(cutoff=1e-10, maxdim=16)
+    kws = dict(updater_kwargs=dict(krylovdim=3, maxiter=1), inserter_kwargs=dict(trunc=trunc))
+    from networksolvers_gb300.sweep import EigsolveProblem, _prepare, sweep_solve, updater_eigsolve
+
+    def run(mod, prep, Problem, solve, upd, plan_fn):
+        psi, P = prep(H, psi0)
+        prob = Problem(psi, P)
+        rec = []
+
+        def cb(prob, sweep, region, which, **k):
+            rec.append((prob.eigenvalue, prob.last_insert.get("newdim", -1)))
+
+        plans = [plan_fn(psi.g, nsites, **kws) for _ in range(3)]
+        prob = solve(prob, plans, upd, region_callback=cb)
+        return np.array(rec), prob.eigenvalue
+
+    r, E = run(pn, lambda H_, p_: _prepare(H_, p_, nsg_ctx), EigsolveProblem, sweep_solve, updater_eigsolve,
+               pn.post_order_dfs_plan)
+    ro, Eo = run(on, osw._prepare, osw.EigsolveProblem, osw.sweep_solve, osw.updater_eigsolve,
+                 on.post_order_dfs_plan)
+    assert np.array_equal(r[:, 1], ro[:, 1])
+    assert np.max(np.abs(r[:, 0] - ro[:, 0]) / np.abs(ro[:, 0])) < 1e-10
+    assert abs(E - Eo) / abs(Eo) < 1e-10
