@@ -246,7 +246,9 @@ def run_nsg(args):
     if rank == 0 and not args.no_e2e:
         arrays = prob.state.to_numpy(psi0)
         from networksolvers_gb300.models import Network
-        host_state = Network(psi0.graph, arrays, psi0.legs, np.float64, {"kind": "state", "ortho_region": list(psi0.graph.vertices)})
+        # the host copy keeps the state's gauge (its orthogonality centre), as a TTN does
+        host_state = Network(psi0.graph, arrays, psi0.legs, np.float64,
+                             {"kind": "state", "ortho_region": list(prob.state.ortho_region)})
         h2d = sum(a.nbytes for a in arrays.values()) + sum(t.nbytes for t in H.tensors.values())
         off = min(args.warmup + args.steps, len(SCHEDULE)) - 1
         kw2 = kwargs_for(off)
