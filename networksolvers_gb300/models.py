@@ -24,7 +24,6 @@ Operator tensors hold ``W[..., s', s] = <s'|O|s>``.  Site basis for S=1/2 is
 from __future__ import annotations
 
 from dataclasses import dataclass, field
-import math
 import numpy as np
 
 # ----------------------------------------------------------------------------

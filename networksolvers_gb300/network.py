@@ -20,7 +20,7 @@ import itertools
 import numpy as np
 
 from . import _native as N
-from .itensors import (DTensor, Index, Storage, contract, uniqueinds, commonind, qr, inner as dinner)
+from .itensors import (DTensor, Index, contract, uniqueinds, commonind, qr)
 
 _stamp = itertools.count(1)
 

@@ -21,7 +21,7 @@ import numpy as np
 
 from . import _native as N
 from .itensors import (DTensor, commonind, uniqueinds, factorize, qr, eigen_hermitian, directsum)
-from .network import (G, TTN, ProjTTN, LinearMap, from_network, orthogonalize, euler_sweep,
+from .network import (TTN, ProjTTN, LinearMap, from_network, orthogonalize, euler_sweep,
                       tdvp_regions, edge_sequence_between_regions)
 
 

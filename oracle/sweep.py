@@ -11,10 +11,10 @@ import math
 
 import numpy as np
 
-from .tensor import Tensor, commonind, uniqueinds, commoninds
+from .tensor import Tensor, commonind, uniqueinds
 from . import linalg, krylov
-from .network import (G, TTN, ProjTTN, from_network, orthogonalize, optimal_map,
-                      euler_sweep, tdvp_regions, edge_sequence_between_regions, inner)
+from .network import (TTN, ProjTTN, from_network, orthogonalize, optimal_map,
+                      euler_sweep, tdvp_regions, edge_sequence_between_regions)
 
 
 # ----------------------------------------------------------------------------

@@ -10,7 +10,6 @@ import pytest
 from networksolvers_gb300 import itensors as it
 from networksolvers_gb300.itensors import DTensor, Index, contract
 from oracle import krylov as ok, linalg as ol
-from oracle.tensor import Index as OIndex, Tensor as OTensor
 
 pytestmark = pytest.mark.gpu
 

@@ -4,7 +4,6 @@ the error of FP32 accumulation over K up to a few thousand."""
 import numpy as np
 import pytest
 
-from networksolvers_gb300 import _native
 from networksolvers_gb300.itensors import DTensor, Index, contract
 
 pytestmark = pytest.mark.gpu

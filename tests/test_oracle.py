@@ -1,7 +1,6 @@
 """The oracle pinned against exact diagonalisation and the reference's own assertions
 (test/dmrg/test_tree_dmrg.jl:53,67; test/tdvp/test_tree_tdvp.jl:65-77)."""
 import numpy as np
-import pytest
 
 import networksolvers_gb300.models as m
 from oracle import sweep, ed, linalg, network
