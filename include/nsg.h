@@ -182,12 +182,16 @@ int nsg_eigh(nsg_ctx* ctx, const nsg_tensor* rho, const int* row_axes, int n_row
  * inserter, inserter.jl:3-33), composed of the entry points above:
  *   L [a', wl, a], W1 [wl, s1', s1, wm], W2 [wm, s2', s2, wr], R [b', wr, b] (the fixed
  *   tensors of optimal_map, operator_map.jl:3-10), psi1 [a, s1, c], psi2 [c, s2, b].
- * Outputs U [a, s1, k] (new psi1, left-orthonormal), C [k, s2, b] (new psi2), the
- * Lanczos eigenvalue, the new bond dimension k and the relative discarded weight. */
+ * Outputs: the new site tensors left [a, s1, k] and right [k, s2, b], the Lanczos
+ * eigenvalue, the new bond dimension k and the relative discarded weight.  direction 0
+ * (region (v1, v2) of a left-to-right pass): left = U is left-orthonormal, right = C;
+ * direction 1 (region (v2, v1) of a right-to-left pass): right = U is right-orthonormal,
+ * left = C (inserter.jl:23 factorizes on the indices of the region's first vertex). */
 int nsg_region_step(nsg_ctx* ctx, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, nsg_tensor* R,
-                    const nsg_tensor* psi1, const nsg_tensor* psi2, int krylovdim, int maxiter,
-                    double tol, double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
-                    nsg_tensor** C, double* energy, int64_t* newdim, double* truncerr);
+                    const nsg_tensor* psi1, const nsg_tensor* psi2, int direction, int krylovdim,
+                    int maxiter, double tol, double cutoff, int64_t maxdim, int64_t mindim,
+                    nsg_tensor** left, nsg_tensor** right, double* energy, int64_t* newdim,
+                    double* truncerr);
 
 /* ---- allocation-free GEMM -------------------------------------------------
  * No counterpart in the reference: an addition for callers that must not allocate

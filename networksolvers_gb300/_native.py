@@ -44,7 +44,8 @@ _SIGS = {
     "nsg_ctx_synchronize": (i32, [p]),
     "nsg_ctx_memory": (i32, [p, C.POINTER(u64), C.POINTER(u64), C.POINTER(u64)]),
     "nsg_device_memory": (i32, [i32, C.POINTER(u64), C.POINTER(u64)]),
-    "nsg_region_step": (i32, [p, p, p, p, p, p, p, i32, i32, dbl, dbl, i64, i64, P_p, P_p, P_dbl, C.POINTER(i64), P_dbl]),
+    "nsg_region_step": (i32, [p, p, p, p, p, p, p, i32, i32, i32, dbl, dbl, i64, i64, P_p, P_p, P_dbl, C.POINTER(i64),
+                              P_dbl]),
     "nsg_ctx_counters": (i32, [p, C.POINTER(u64), i32]),
     "nsg_ctx_event_record": (i32, [p, i32]),
     "nsg_ctx_event_elapsed": (i32, [p, i32, i32, C.POINTER(C.c_float)]),

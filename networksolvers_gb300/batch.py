@@ -106,11 +106,28 @@ def tdvp_job(H, psi0, time_points, tag=None, arrival=0.0, maxdim=64, cutoff=1e-9
     return Job("tdvp", H, psi0, kw, tag, arrival)
 
 
+def _is_chain(graph):
+    vs = sorted(graph.vertices)
+    n = len(vs)
+    return vs == list(range(1, n + 1)) and all(
+        sorted(graph.neighbors(v)) == [u for u in (v - 1, v + 1) if 1 <= u <= n] for v in vs)
+
+
 def _run_job(job: Job, ctx):
     from .sweep import eigsolve, tdvp
     kw = dict(job.kwargs)
     if job.kind == "dmrg":
         nsweeps = kw.pop("nsweeps")
+        ex = kw.get("extracter_kwargs") or {}
+        if kw.get("nsites", 1) == 2 and not ex.get("subspace_algorithm") and _is_chain(job.psi0.graph):
+            # plain two-site chain DMRG: the fused per-region driver (same results)
+            from .chain import dmrg_chain
+            up = kw.get("updater_kwargs") or {}
+            tr = (kw.get("inserter_kwargs") or {}).get("trunc") or {}
+            E, _, _ = dmrg_chain(job.H, job.psi0, nsweeps, maxdim=tr.get("maxdim"), cutoff=tr.get("cutoff", 0.0),
+                                 mindim=tr.get("mindim", 1), krylovdim=up.get("krylovdim", 3),
+                                 maxiter=up.get("maxiter", 1), tol=up.get("tol", 1e-14), ctx=ctx)
+            return float(E)
         E, _ = eigsolve(job.H, job.psi0, nsweeps, ctx=ctx, **kw)
         return float(E)
     if job.kind == "tdvp":

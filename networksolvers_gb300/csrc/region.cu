@@ -14,11 +14,12 @@ using namespace nsg;
 extern "C" {
 
 int nsg_region_step(nsg_ctx* c, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, nsg_tensor* R,
-                    const nsg_tensor* psi1, const nsg_tensor* psi2, int krylovdim, int maxiter, double tol,
-                    double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U, nsg_tensor** C,
-                    double* energy, int64_t* newdim, double* truncerr) {
+                    const nsg_tensor* psi1, const nsg_tensor* psi2, int direction, int krylovdim, int maxiter,
+                    double tol, double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** left,
+                    nsg_tensor** right, double* energy, int64_t* newdim, double* truncerr) {
   NSG_API_BEGIN(c)
-  NSG_CHECK(c && L && W1 && W2 && R && psi1 && psi2 && U && C && energy, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(c && L && W1 && W2 && R && psi1 && psi2 && left && right && energy, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(direction == 0 || direction == 1, NSG_ERR_INVALID, "region_step: direction 0 or 1");
   NSG_CHECK(L->rank == 3 && R->rank == 3 && W1->rank == 4 && W2->rank == 4 && psi1->rank == 3 && psi2->rank == 3,
             NSG_ERR_INVALID, "region_step: ranks must be L 3, W1 4, W2 4, R 3, psi1 3, psi2 3");
   // labels: a, a', wl, s1, s1', wm, s2, s2', wr, b, b', c (the bond between the sites)
@@ -51,10 +52,31 @@ int nsg_region_step(nsg_ctx* c, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, n
     nsg_tensor_release(c, local);
     throw Error(rc, std::string("region_step: ") + c->err);
   }
-  const int left[2] = {0, 1};
-  rc = nsg_factorize(c, local, left, 2, cutoff, maxdim, mindim, U, C, newdim, truncerr, nullptr, 0);
+  // direction 0 (left-to-right): U [a, s1, k] -> left site, C [k, s2, b] -> right site.
+  // direction 1 (right-to-left, region (v2, v1) of the plan): the factorization keeps
+  // the right site's indices with U: U [s2, b, k] -> right site as [k, s2, b],
+  // C [k, a, s1] -> left site as [a, s1, k].
+  const int axes0[2] = {0, 1}, axes1[2] = {2, 3};
+  nsg_tensor *U = nullptr, *Cf = nullptr;
+  rc = nsg_factorize(c, local, direction == 0 ? axes0 : axes1, 2, cutoff, maxdim, mindim, &U, &Cf, newdim, truncerr,
+                     nullptr, 0);
   nsg_tensor_release(c, local);
   NSG_CHECK(rc == NSG_OK, rc, std::string("region_step: ") + c->err);
+  if (direction == 0) {
+    *left = U;
+    *right = Cf;
+  } else {
+    const int pu[3] = {2, 0, 1}, pc[3] = {1, 2, 0};
+    const int64_t du[3] = {U->dims[2], U->dims[0], U->dims[1]}, dc[3] = {Cf->dims[1], Cf->dims[2], Cf->dims[0]};
+    nsg_tensor* Ur = new_tensor(c, U->dtype, 3, du, false);
+    nsg_tensor* Cl = new_tensor(c, Cf->dtype, 3, dc, false);
+    permute(c, U, pu, false, Ur);
+    permute(c, Cf, pc, false, Cl);
+    free_tensor(c, U);
+    free_tensor(c, Cf);
+    *left = Cl;
+    *right = Ur;
+  }
   NSG_API_END(c)
 }
 

@@ -262,20 +262,22 @@ def inserter(problem, local, region_iterator, sweep, normalize=False, set_orthog
     return problem
 
 
-def region_step(L, W1, W2, R, psi1, psi2, krylovdim=3, maxiter=1, tol=1e-14, cutoff=0.0, maxdim=None, mindim=1,
-                tags="Link"):
+def region_step(L, W1, W2, R, psi1, psi2, direction=0, krylovdim=3, maxiter=1, tol=1e-14, cutoff=0.0, maxdim=None,
+                mindim=1, tags="Link"):
     """One fused two-site region step (nsg_region_step): psi1·psi2, Lanczos on the H_eff of
     [L, R, W1, W2], truncated factorization — the extracter / updater / inserter of one
     chain region in a single library call.  Layout: L [a', wl, a], W1 [wl, s1', s1, wm],
-    W2 [wm, s2', s2, wr], R [b', wr, b], psi1 [a, s1, c], psi2 [c, s2, b].
-    Returns (energy, U [a, s1, k], C [k, s2, b], info)."""
+    W2 [wm, s2', s2, wr], R [b', wr, b], psi1 [a, s1, c], psi2 [c, s2, b].  direction 0:
+    the new left tensor is left-orthonormal; 1: the new right tensor is right-orthonormal.
+    Returns (energy, left [a, s1, k], right [k, s2, b], info)."""
     from .itensors import Index, Storage
     ctx = psi1.ctx
     ts = [t.materialize() for t in (L, W1, W2, R, psi1, psi2)]
     U, Cc = C.c_void_p(), C.c_void_p()
     E, k, err = C.c_double(), C.c_int64(), C.c_double()
     md = -1 if maxdim is None else int(maxdim)
-    ctx.check(ctx.L.nsg_region_step(ctx.h, *[t.st.h for t in ts], int(krylovdim), int(maxiter), float(tol),
+    ctx.check(ctx.L.nsg_region_step(ctx.h, *[t.st.h for t in ts], int(direction), int(krylovdim), int(maxiter),
+                                    float(tol),
                                     float(cutoff), md, int(mindim), C.byref(U), C.byref(Cc), C.byref(E),
                                     C.byref(k), C.byref(err)))
     p1, p2 = ts[4], ts[5]

@@ -334,7 +334,8 @@ def test_fused_region_step_matches_call_by_call(nsg_ctx):
     W2 = DTensor.from_numpy(W, [w2, s2.prime(), s2, w3])
     p1 = DTensor.from_numpy(rng.standard_normal((chi, d, chi)), [a, s1, cc])
     p2 = DTensor.from_numpy(rng.standard_normal((chi, d, chi)), [cc, s2, b])
-    E1, U1, C1, info1 = region_step(L, W1, W2, R, p1, p2, krylovdim=3, maxiter=1, cutoff=1e-10, maxdim=30)
+    E1, U1, C1, info1 = region_step(L, W1, W2, R, p1, p2, direction=0, krylovdim=3, maxiter=1, cutoff=1e-10,
+                                    maxdim=30)
     local = contract([p1, p2], out=[a, s1, s2, b])
     lm = LinearMap(_FixedMap([L, R, W1, W2]), [a, s1, s2, b])
     E2, x = eigsolve_solver(lm, local, krylovdim=3, maxiter=1)

@@ -256,3 +256,29 @@ def test_tree_dmrg_with_jumping_post_order_plan(nsg_ctx, nsites):
     assert np.array_equal(r[:, 1], ro[:, 1])
     assert np.max(np.abs(r[:, 0] - ro[:, 0]) / np.abs(ro[:, 0])) < 1e-10
     assert abs(E - Eo) / abs(Eo) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_chain_driver_matches_general_driver(nsg_ctx, precision):
+    """The chain driver (one fused region-step call per region) against the general
+    driver on a J1-J2 chain with a maxdim schedule: per-region energies 1e-11 relative,
+    identical bond dimensions, the same final state up to rounding."""
+    from networksolvers_gb300.chain import dmrg_chain
+    n = 16
+    H = m.j1j2_chain(n, 0.3)
+    psi0 = m.random_state(m.chain_graph(n), 8, seed=7)
+    trunc = dict(cutoff=1e-10, maxdim=[16, 32, 64])
+    nsg_ctx.set_precision(precision)
+    try:
+        Eg, rg, psig = _record_dmrg(ns.dmrg, H, psi0, nsweeps=3, nsites=2,
+                                    updater_kwargs=dict(krylovdim=3, maxiter=1), inserter_kwargs=dict(trunc=trunc))
+        Ec, tens, rec = dmrg_chain(H, psi0, 3, maxdim=[16, 32, 64], cutoff=1e-10, ctx=nsg_ctx)
+    finally:
+        nsg_ctx.set_precision("fp64")
+    rc = np.array([(e, k) for (_, _, e, k) in rec])
+    assert np.array_equal(rc[:, 1], rg[:, 3])
+    assert np.max(np.abs(rc[:, 0] - rg[:, 2]) / np.abs(rg[:, 2])) < 1e-11
+    assert abs(Ec - Eg) / abs(Eg) < 1e-11
+    ref = psig.to_numpy(psi0)
+    for v in ref:
+        assert tens[v].shape == ref[v].shape
