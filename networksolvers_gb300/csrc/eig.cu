@@ -9,6 +9,10 @@
 // ortho="left" stores (U -> psi[v1], C -> psi[v2]).  m > n: the narrow side's Gram
 // matrix M^H M = V S^2 V^H, U = M V S^-1 re-orthogonalised, C = U^H M.  The Hermitian
 // eigenproblems go to the tridiagonalisation + divide-and-conquer solver (syevd.cu).
+// Every product here is FP64-level: the FP64 cores, or in the split precision the
+// eight-slice Ozaki form (real data), whose error is at the FP64 rounding level of the
+// operand scales; the Gram matrix stays exactly symmetric in both (same slices on both
+// sides, exact integer partial sums).
 //
 // Truncation rule (NDTensors, restated): spectrum P = lambda sorted descending,
 // negative tail zeroed; cut to maxdim; then drop from the end while
@@ -170,7 +174,7 @@ static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, 
   g.ldc = n;
   g.batch = 1;
   g.strideA = g.strideB = g.strideC = 0;
-  gemm_f64_simt(c, g);  // FP64 in every precision mode: the Gram matrix fixes the truncation
+  gemm_accurate(c, g);  // FP64-level product: the Gram matrix fixes the truncation
   int64_t k = 0;
   double err = 0.0, delta = 0.0;
   bool ok = true;
@@ -358,7 +362,7 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
       return NSG_OK;
     }
   }
-  // G = M M^H (FP64 in every precision mode: the Gram matrix fixes the truncation)
+  // G = M M^H (FP64-level product in every precision mode: the Gram matrix fixes the truncation)
   void* G = dalloc(c, eb * m * m);
   GemmArgs g;
   g.dtype = dt;
@@ -375,7 +379,7 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   g.ldc = m;
   g.batch = 1;
   g.strideA = g.strideB = g.strideC = 0;
-  gemm_f64_simt(c, g);
+  gemm_accurate(c, g);
   const int64_t origm = std::min(m, ncol);
   double err = 0.0;
   int64_t k = 0;

@@ -93,41 +93,14 @@ __device__ __forceinline__ double2 fcma(double2 acc, double2 a, double2 b) {
   return make_double2(fma(a.y, b.y, fma(a.x, b.x, acc.x)), fma(-a.y, b.x, fma(a.x, b.y, acc.y)));
 }
 
-// Grid barrier with a bounded wait (cooperative launch guarantees co-residency).
+// Grid barrier state of the tridiagonalisation (cooperative launch guarantees
+// co-residency): a monotonic arrival counter (every CTA knows how many arrivals close
+// each step, so nothing is reset between steps) and an error flag set by a wait that
+// gave up.
 struct Barrier {
   unsigned int count;
-  unsigned int gen;
   int err;
 };
-
-__device__ bool grid_sync(Barrier* b) {
-  __shared__ int s_ok;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    volatile unsigned int* vgen = &b->gen;
-    unsigned int g = *vgen;
-    __threadfence();
-    unsigned int arrived = atomicAdd(&b->count, 1u);
-    if (arrived == gridDim.x - 1) {
-      b->count = 0;
-      __threadfence();
-      atomicAdd(&b->gen, 1u);
-    } else {
-      long long polls = 0;
-      while (*vgen == g) {
-        if (++polls > (1ll << 26) || *(volatile int*)&b->err) {
-          atomicExch(&b->err, 1);
-          break;
-        }
-        __nanosleep(32);
-      }
-    }
-    __threadfence();
-    s_ok = (*(volatile int*)&b->err) == 0;
-  }
-  __syncthreads();
-  return s_ok;
-}
 
 template <typename T>
 __device__ T block_sum(T v, T* red) {
@@ -160,6 +133,9 @@ __device__ T block_sum(T v, T* red) {
 // rebuilds the updated pivot column itself, and one pass over the trailing block both
 // applies the pending update and forms step k's x (one grid barrier per column).  CTAs
 // retire as the trailing block shrinks (the barrier target follows the active count).
+// A step is a chain of dependent L2 round trips, so the loads it needs are issued
+// together: right after a barrier the next pivot column, x and the CTAs' partial sums,
+// and at the top of a step the first tile of its pass.
 template <typename T, int NT>
 __global__ void __launch_bounds__(NT)
     tridiag_kernel(T* __restrict__ A, int n, double* __restrict__ d, double* __restrict__ e, T* __restrict__ tau,
@@ -171,10 +147,24 @@ __global__ void __launch_bounds__(NT)
   __shared__ T red[NT / 32];
   __shared__ double2 wsum[NT / 32];
   __shared__ T part_s[kTriUnits];  // per-unit partial dot products of the pass
+  __shared__ int s_ok;
   constexpr int nt = NT, nwarps = NT / 32;
+  constexpr int P = sizeof(T) == 8 ? 8 : 4;  // pivot-column and x entries per thread held in registers
+  constexpr int PQ = 8;                      // CTA partial sums per lane held in registers
+  constexpr int U = sizeof(T) == 8 ? 16 : 8, RB = 32 * U;
   const int tid = threadIdx.x, b = blockIdx.x;
   const int warp = tid >> 5, lane = tid & 31;
   bool has_prev = false;
+  unsigned int target = 0;  // arrivals on the barrier counter that close the current step
+  // step 0's pivot column as stored: rows 1 + tid + j nt, and the diagonal
+  T raw[P];
+  T rawd = czero<T>();
+#pragma unroll
+  for (int j = 0; j < P; ++j) {
+    const int r = tid + j * nt;
+    raw[j] = r < n - 1 ? __ldcg(A + 1 + r) : czero<T>();
+  }
+  if (b == 0 && tid == 0) rawd = __ldcg(A);
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;  // trailing size (rows k+1..n-1)
     int nact = int(((int64_t)m * m + (int64_t)nt * per_thread - 1) / ((int64_t)nt * per_thread));
@@ -185,23 +175,44 @@ __global__ void __launch_bounds__(NT)
     // barrier keeps every CTA within one step of the others)
     T* xb = xbuf + (size_t)(k & 1) * n;
     double2* pb = (double2*)partial + (size_t)(k & 1) * gridDim.x;
+    // the CTA's columns [j0, j1) of the trailing block, in work units of one column x RB
+    // rows dealt to the warps round-robin; the block is final since the last barrier, so
+    // each warp's first unit is requested before the pivot column is reduced
+    const int j0 = int((int64_t)m * b / nact), j1 = int((int64_t)m * (b + 1) / nact);
+    const int ncol = j1 - j0, nrb = (m + RB - 1) / RB, nunits = ncol * nrb;
+    T cur[U], nxt[U];
+    auto load_unit = [&](int u, T* dst) {
+      const int q = u / nrb, rb = u - q * nrb;
+      const T* cj = A + (size_t)(k + 1 + j0 + q) * n + (k + 1);
+#pragma unroll
+      for (int t = 0; t < U; ++t) {
+        const int r = rb * RB + 32 * t + lane;
+        dst[t] = r < m ? __ldcg(cj + r) : czero<T>();
+      }
+    };
+    if (warp < nunits) load_unit(warp, cur);
     // 1. pivot column k with the pending update applied (rows k..n-1), reflector
     const T* colk = A + (size_t)k * n;
     const T wp0 = has_prev ? cconj(wprev[0]) : czero<T>();
     const T vp0 = has_prev ? cconj(vprev[0]) : czero<T>();
-    auto colval = [&](int i) -> T {  // i >= k
-      T a = __ldcg(colk + i);
-      if (has_prev) a = fnms2(a, vprev[i - k], wp0, wprev[i - k], vp0);
-      return a;
-    };
-    // one read of the pivot column: vcur holds it until the reflector is known
     T dk = czero<T>();
-    if (b == 0 && tid == 0) dk = colval(k);
+    if (b == 0 && tid == 0) dk = has_prev ? fnms2(rawd, vprev[0], wp0, wprev[0], vp0) : rawd;
     double ss = 0.0;
-    for (int r = tid; r < m; r += nt) {
-      const T a = colval(k + 1 + r);
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      const int r = tid + j * nt;
+      if (r < m) {
+        T a = raw[j];
+        if (has_prev) a = fnms2(a, vprev[r + 1], wp0, wprev[r + 1], vp0);
+        vcur[r] = a;
+        if (r > 0) ss += cabs2(a);
+      }
+    }
+    for (int r = tid + P * nt; r < m; r += nt) {  // orders above P nt + 1: loaded here
+      T a = __ldcg(colk + k + 1 + r);
+      if (has_prev) a = fnms2(a, vprev[r + 1], wp0, wprev[r + 1], vp0);
       vcur[r] = a;
-      if (r > 0) ss += cabs2(a);
+      ss += cabs2(a);
     }
     const double xnorm2 = block_sum<double>(ss, (double*)red);  // its barriers publish vcur
     const T alpha = vcur[0];
@@ -234,26 +245,10 @@ __global__ void __launch_bounds__(NT)
       e[k] = active ? beta : ar;
       tau[k] = tk;
     }
-    // 2. the CTA's columns [j0, j1) of the trailing block: pending update, then
-    //    x_j = tau * A22[:, j]^H v.  Work units (one column x RB rows) are dealt to the
-    //    warps round-robin, so the warps carry equal loads; a warp loads its next unit
-    //    before it updates and stores the current one (units are disjoint).  The trailing
-    //    block is rewritten by other CTAs between steps: every access bypasses L1.
+    // 2. the pass: pending update, then x_j = tau * A22[:, j]^H v.  A warp loads its next
+    //    unit before it updates and stores the current one (units are disjoint).  The
+    //    trailing block is rewritten by other CTAs between steps: every access bypasses L1.
     {
-      constexpr int U = sizeof(T) == 8 ? 16 : 8, RB = 32 * U;
-      const int j0 = int((int64_t)m * b / nact), j1 = int((int64_t)m * (b + 1) / nact);
-      const int ncol = j1 - j0, nrb = (m + RB - 1) / RB, nunits = ncol * nrb;
-      T cur[U], nxt[U];
-      auto load_unit = [&](int u, T* dst) {
-        const int q = u / nrb, rb = u - q * nrb;
-        const T* cj = A + (size_t)(k + 1 + j0 + q) * n + (k + 1);
-#pragma unroll
-        for (int t = 0; t < U; ++t) {
-          const int r = rb * RB + 32 * t + lane;
-          dst[t] = r < m ? __ldcg(cj + r) : czero<T>();
-        }
-      };
-      if (warp < nunits) load_unit(warp, cur);
       for (int u = warp; u < nunits; u += nwarps) {
         if (u + nwarps < nunits) load_unit(u + nwarps, nxt);
         const int q = u / nrb, rb = u - q * nrb, jj = j0 + q;
@@ -322,43 +317,60 @@ __global__ void __launch_bounds__(NT)
         __stcg(pb + b, sacc);
       }
     }
-    // 3. barrier among the active CTAs
-    {
-      __shared__ int s_ok;
-      __syncthreads();
-      if (tid == 0) {
-        volatile unsigned int* vgen = &bar->gen;
-        unsigned int g = *vgen;
-        __threadfence();
-        unsigned int arrived = atomicAdd(&bar->count, 1u);
-        if (arrived == (unsigned)nact - 1) {
-          bar->count = 0;
-          __threadfence();
-          atomicAdd(&bar->gen, 1u);
-        } else {
-          long long polls = 0;
-          while (*vgen == g) {
-            if (++polls > (1ll << 26) || *(volatile int*)&bar->err) {
-              atomicExch(&bar->err, 1);
-              break;
-            }
-            __nanosleep(20);
-          }
+    // 3. barrier among the active CTAs: every CTA active now was active in every earlier
+    //    step (the active count never grows), so all of them agree on the target
+    target += unsigned(nact);
+    __syncthreads();
+    if (tid == 0) {
+      __threadfence();
+      atomicAdd(&bar->count, 1u);
+      volatile unsigned int* vcount = &bar->count;
+      long long polls = 0;
+      while (int(*vcount - target) < 0) {
+        if (++polls > (1ll << 26) || *(volatile int*)&bar->err) {
+          atomicExch(&bar->err, 1);
+          break;
         }
-        __threadfence();
-        s_ok = (*(volatile int*)&bar->err) == 0;
+        __nanosleep(20);
       }
-      __syncthreads();
-      if (!s_ok) return;
+      __threadfence();
+      s_ok = (*(volatile int*)&bar->err) == 0;
     }
-    // 4. w = x + alpha2 v becomes the pending update (relative to rows >= k+1); the
-    // loads of x and of the partials are issued together
-#pragma unroll 4
-    for (int r = tid; r < m; r += nt) wprev[r] = __ldcg(xb + r);
-    // every warp sums the CTAs' partials (lane-strided, then a butterfly: the same value
-    // in every lane of every CTA)
+    __syncthreads();
+    if (!s_ok) return;
+    // 4. requested together: x, the CTAs' partials of x^H v, and the next pivot column
+    //    (column k+1: rows k+2.. and its diagonal) as the pass above stored it
+    T xr[P];
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      const int r = tid + j * nt;
+      xr[j] = r < m ? __ldcg(xb + r) : czero<T>();
+    }
+    double2 pq[PQ];
+#pragma unroll
+    for (int j = 0; j < PQ; ++j) {
+      const int q = lane + 32 * j;
+      pq[j] = q < nact ? __ldcg(pb + q) : make_double2(0.0, 0.0);
+    }
+    {
+      const T* coln = A + (size_t)(k + 1) * n + (k + 2);
+#pragma unroll
+      for (int j = 0; j < P; ++j) {
+        const int r = tid + j * nt;
+        raw[j] = r < m - 1 ? __ldcg(coln + r) : czero<T>();
+      }
+      if (b == 0 && tid == 0) rawd = __ldcg(A + (size_t)(k + 1) * n + (k + 1));
+    }
+    for (int r = tid + P * nt; r < m; r += nt) wprev[r] = __ldcg(xb + r);
+    // every warp sums the CTAs' partials (lane-strided in ascending order, then a
+    // butterfly: the same value in every lane of every CTA)
     double2 xv = make_double2(0.0, 0.0);
-    for (int q = lane; q < nact; q += 32) {
+#pragma unroll
+    for (int j = 0; j < PQ; ++j) {
+      xv.x += pq[j].x;
+      xv.y += pq[j].y;
+    }
+    for (int q = lane + 32 * PQ; q < nact; q += 32) {
       const double2 t = __ldcg(pb + q);
       xv.x += t.x;
       xv.y += t.y;
@@ -379,8 +391,17 @@ __global__ void __launch_bounds__(NT)
     // before the barrier, and it is not read again
     if (b == 0)
       for (int r = tid + 1; r < m; r += nt) A[(size_t)k * n + (k + 1 + r)] = vcur[r];
-    __syncthreads();
-    for (int r = tid; r < m; r += nt) {  // the entries this thread loaded above
+    // 5. w = x + alpha2 v becomes the pending update (relative to rows >= k+1); a thread
+    //    rewrites only the entries it holds
+#pragma unroll
+    for (int j = 0; j < P; ++j) {
+      const int r = tid + j * nt;
+      if (r < m) {
+        vprev[r] = vcur[r];
+        wprev[r] = active ? cadd(xr[j], cmulv(alpha2, vcur[r])) : czero<T>();
+      }
+    }
+    for (int r = tid + P * nt; r < m; r += nt) {
       vprev[r] = vcur[r];
       wprev[r] = active ? cadd(wprev[r], cmulv(alpha2, vcur[r])) : czero<T>();
     }
