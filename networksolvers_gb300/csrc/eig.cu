@@ -337,7 +337,14 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
     }
     scale(c, dt, M->size, 1.0 / sc, 0.0, M->data);
   }
-  if (ncol < m && ncol >= 16) {
+  // The tall route is kept only when its smallest kept sigma^2 lies above 1e-11 of the
+  // largest (checked once the spectrum is known, before any eigenvector is formed).  A
+  // truncation that only the cutoff limits keeps weights down to ~cutoff / (discarded
+  // count) of the total, so with cutoff < 1e-10 and no maxdim below the narrow side the
+  // check fails on practically every spectrum: the attempt (Gram matrix, tridiagonal
+  // reduction and divide and conquer of the narrow side) is then skipped.
+  const bool tall_may_pass = cutoff >= 1e-10 || (maxdim > 0 && maxdim < ncol);
+  if (ncol < m && ncol >= 16 && tall_may_pass) {
     std::vector<double> Pr;
     nsg_tensor *Ur = nullptr, *Cr = nullptr;
     int64_t kr = 0;
