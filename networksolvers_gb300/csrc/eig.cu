@@ -111,18 +111,29 @@ __global__ void col_scale_kernel(T* Y, int64_t rows, int64_t cols, const double*
   }
 }
 
-// G <- 1.5 I - 0.5 G (k x k): the first-order inverse square root of a Gram matrix
-// that is the identity up to small terms (symmetric re-orthogonalisation)
+// D <- G - I (k x k): the deviation of a Gram matrix from the identity
 template <typename T>
-__global__ void half_newton_kernel(T* G, int64_t k) {
+__global__ void sub_identity_kernel(T* G, int64_t k) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < k; i += int64_t(gridDim.x) * blockDim.x) {
+    if constexpr (sizeof(T) == 8)
+      G[i * k + i] -= 1.0;
+    else
+      G[i * k + i].x -= 1.0;
+  }
+}
+
+// D <- I - D / 2 with D = G - I: the first-order inverse square root (3 I - G) / 2 of a
+// Gram matrix that is the identity up to small terms (symmetric re-orthogonalisation)
+template <typename T>
+__global__ void newton_step_kernel(T* D, int64_t k) {
   const int64_t tot = k * k;
   for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
     const bool diag = (e % k) == (e / k);
     if constexpr (sizeof(T) == 8) {
-      G[e] = (diag ? 1.5 : 0.0) - 0.5 * G[e];
+      D[e] = (diag ? 1.0 : 0.0) - 0.5 * D[e];
     } else {
-      G[e].x = (diag ? 1.5 : 0.0) - 0.5 * G[e].x;
-      G[e].y = -0.5 * G[e].y;
+      D[e].x = (diag ? 1.0 : 0.0) - 0.5 * D[e].x;
+      D[e].y = -0.5 * D[e].y;
     }
   }
 }
@@ -144,13 +155,19 @@ struct DevBuf1 {
 }  // namespace
 
 // Tall M (m > ncol): truncated factorisation from the smaller Gram matrix M^H M
-// = V S^2 V^H.  U = M V_k S_k^{-1} carries a relative column error ~ eps s_max / s_k,
-// removed by symmetric re-orthogonalisation U <- U (3 I - U^H U) / 2 (each step squares
-// it; two steps when eps s_max / s_k > 1e-8); C = U^H M as in the square route.  The
-// spectrum and the truncation rule are those of M M^H (same non-zero eigenvalues).
-// Returns false, having allocated nothing that outlives it, when s_k^2 <= 1e-11 s_max^2
-// (s_k not resolved by the Gram matrix well above its rounding): the caller then takes
-// the M M^H route.
+// = V S^2 V^H; the spectrum and the truncation rule are those of M M^H (same non-zero
+// eigenvalues), C = U^H M as in the square route.  U = M V_k S_k^{-1}, in two parts:
+//  * resolved columns (s_i^2 > 1e-11 s_max^2): accurate up to rotations among nearby
+//    small singular directions (relative size eps s_max^2 / gap); symmetric
+//    re-orthogonalisation U <- U (3 I - U^H U) / 2, repeated until U^H U = I to 1e-14;
+//  * the tail below (singular values the Gram matrix resolves only to its rounding):
+//    these columns span the right small-singular space but as an ill-conditioned basis;
+//    they are projected off the resolved columns twice and orthonormalised through the
+//    eigen-decomposition of their own Gram matrix (W <- W E D^-1/2 E^H), then the whole U
+//    gets the same re-orthogonalisation.
+// Returns false, having allocated nothing that outlives it, when the tail is exactly rank
+// deficient, a kept weight is not positive, or the tail's eigenproblem would make the
+// route dearer than M M^H (tail + ncol > m): the caller then takes the M M^H route.
 static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, const std::vector<int64_t>& ldims,
                             const std::vector<int64_t>& rdims, double sc, double cutoff, int64_t maxdim,
                             int64_t mindim, nsg_tensor** Uo, nsg_tensor** Co, int64_t* ko, double* erro,
@@ -158,25 +175,31 @@ static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, 
   const int dt = M->dtype;
   const size_t eb = elem_bytes(dt);
   const int64_t n = ncol;
+  auto mm = [&](int64_t M_, int64_t N_, int64_t K_, const void* A, int64_t lda, int opA, const void* B, int64_t ldb,
+                int opB, void* C, int64_t ldc, double alpha, double beta) {
+    GemmArgs g;
+    g.dtype = dt;
+    g.M = M_;
+    g.N = N_;
+    g.K = K_;
+    g.A = A;
+    g.lda = lda;
+    g.opA = opA;
+    g.B = B;
+    g.ldb = ldb;
+    g.opB = opB;
+    g.C = C;
+    g.ldc = ldc;
+    g.batch = 1;
+    g.strideA = g.strideB = g.strideC = 0;
+    g.alpha_re = alpha;
+    g.beta_re = beta;
+    gemm_accurate(c, g);
+  };
   void* G = dalloc(c, eb * n * n);
-  GemmArgs g;
-  g.dtype = dt;
-  g.M = n;
-  g.N = n;
-  g.K = m;
-  g.A = M->data;
-  g.lda = m;
-  g.opA = OP_C;
-  g.B = M->data;
-  g.ldb = m;
-  g.opB = OP_N;
-  g.C = G;
-  g.ldc = n;
-  g.batch = 1;
-  g.strideA = g.strideB = g.strideC = 0;
-  gemm_accurate(c, g);  // FP64-level product: the Gram matrix fixes the truncation
-  int64_t k = 0;
-  double err = 0.0, delta = 0.0;
+  mm(n, n, m, M->data, m, OP_C, M->data, m, OP_N, G, n, 1.0, 0.0);  // FP64-level: fixes the truncation
+  int64_t k = 0, kr = 0;
+  double err = 0.0;
   bool ok = true;
   void* V = nullptr;
   size_t vbytes = 0;
@@ -184,11 +207,10 @@ static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, 
   PickFn pick = [&](const std::vector<double>& wa, void** Z, int64_t* ldz) {
     P.assign(wa.rbegin(), wa.rend());
     k = truncate_rule(P, n, cutoff, maxdim, mindim, &err);
-    // the Gram eigenvalues carry ~1e-15 P[0] of rounding: s_k must be resolved well above it
-    const double smax = std::sqrt(std::max(P[0], 0.0)), smin = std::sqrt(std::max(P[k - 1], 0.0));
-    ok = smax > 0.0 && P[k - 1] > 1e-11 * P[0];
+    kr = 0;
+    while (kr < k && P[kr] > 1e-11 * P[0]) ++kr;
+    ok = P[0] > 0.0 && P[k - 1] > 0.0 && (k - kr) + n <= m;
     if (!ok) return std::vector<int>();
-    delta = 1e-16 * smax / smin;
     vbytes = eb * size_t(n) * size_t(k);
     V = dalloc(c, vbytes);
     *Z = V;
@@ -206,101 +228,124 @@ static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, 
   }
   dfree(c, G, eb * n * n);
   if (!ok) return false;
-  // Y = M V_k S_k^{-1}
+  // U = M V_k S_k^{-1}
   std::vector<int64_t> udims = ldims;
   udims.push_back(k);
   nsg_tensor* Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
-  GemmArgs y;
-  y.dtype = dt;
-  y.M = m;
-  y.N = k;
-  y.K = n;
-  y.A = M->data;
-  y.lda = m;
-  y.opA = OP_N;
-  y.B = V;
-  y.ldb = n;
-  y.opB = OP_N;
-  y.C = Ut->data;
-  y.ldc = m;
-  y.batch = 1;
-  y.strideA = y.strideB = y.strideC = 0;
-  gemm_accurate(c, y);
+  mm(m, k, n, M->data, m, OP_N, V, n, OP_N, Ut->data, m, 1.0, 0.0);
   dfree(c, V, vbytes);
+  const int gsms = int(c->num_sms) * 8;
+  auto col_scale = [&](void* Y, int64_t rows, int64_t cols, const double* f_dev) {
+    const int gb = int(std::min<int64_t>((rows * cols + 255) / 256, gsms));
+    if (dt == NSG_C128)
+      col_scale_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Y, rows, cols, f_dev);
+    else
+      col_scale_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Y, rows, cols, f_dev);
+    count_launch(c);
+  };
   {
     std::vector<double> inv(k);
     for (int64_t i = 0; i < k; ++i) inv[i] = 1.0 / std::sqrt(P[i]);
     DevBuf1 f(c, sizeof(double) * k);
     NSG_CUDA(cudaMemcpyAsync(f.p, inv.data(), sizeof(double) * k, cudaMemcpyHostToDevice, c->stream));
-    const int gb = int(std::min<int64_t>((m * k + 255) / 256, int64_t(c->num_sms) * 8));
-    if (dt == NSG_C128)
-      col_scale_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Ut->data, m, k, (const double*)f.p);
-    else
-      col_scale_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Ut->data, m, k, (const double*)f.p);
-    count_launch(c);
+    col_scale(Ut->data, m, k, (const double*)f.p);
     NSG_CUDA(cudaStreamSynchronize(c->stream));  // inv leaves scope
   }
-  // symmetric re-orthogonalisation
-  const int iters = delta > 1e-8 ? 2 : 1;
-  nsg_tensor* Y2 = new_tensor(c, dt, int(udims.size()), udims.data(), false);
+  char* U = (char*)Ut->data;
+  const int64_t kt = k - kr;
+  void* Y2 = dalloc(c, eb * m * k);
   void* Gk = dalloc(c, eb * k * k);
-  for (int it = 0; it < iters; ++it) {
-    GemmArgs q = y;
-    q.M = k;
-    q.N = k;
-    q.K = m;
-    q.A = Ut->data;
-    q.lda = m;
-    q.opA = OP_C;
-    q.B = Ut->data;
-    q.ldb = m;
-    q.opB = OP_N;
-    q.C = Gk;
-    q.ldc = k;
-    gemm_accurate(c, q);
-    const int gb = int(std::min<int64_t>((k * k + 255) / 256, int64_t(c->num_sms) * 8));
-    if (dt == NSG_C128)
-      half_newton_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Gk, k);
-    else
-      half_newton_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Gk, k);
-    count_launch(c);
-    GemmArgs r = y;
-    r.M = m;
-    r.N = k;
-    r.K = k;
-    r.A = Ut->data;
-    r.lda = m;
-    r.opA = OP_N;
-    r.B = Gk;
-    r.ldb = k;
-    r.opB = OP_N;
-    r.C = Y2->data;
-    r.ldc = m;
-    gemm_accurate(c, r);
-    std::swap(Ut, Y2);
+  // symmetric re-orthogonalisation of the first kk columns until U^H U = I to the
+  // rounding of the Gram product (or until a step stops gaining); false when U^H U is too
+  // far from I for the iteration to converge, or it ends above 1e-13
+  const double floor_tol = std::max(1e-14, 8.0 * 2.220446049250313e-16 * std::sqrt(double(m)));
+  auto lowdin = [&](int64_t kk) -> bool {
+    double prev = 1.0;
+    for (int it = 0; it < 6; ++it) {
+      mm(kk, kk, m, U, m, OP_C, U, m, OP_N, Gk, kk, 1.0, 0.0);
+      const int gb = int(std::min<int64_t>((kk * kk + 255) / 256, gsms));
+      if (dt == NSG_C128)
+        sub_identity_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Gk, kk);
+      else
+        sub_identity_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Gk, kk);
+      count_launch(c);
+      const double dev = amax(c, dt, kk * kk, Gk);
+      if (!(dev < 0.1 / std::sqrt(double(kk)))) return false;
+      if (dev < floor_tol) return true;
+      if (dev > 0.1 * prev) return dev < 1e-13;  // at the rounding floor
+      prev = dev;
+      if (dt == NSG_C128)
+        newton_step_kernel<double2><<<gb, 256, 0, c->stream>>>((double2*)Gk, kk);
+      else
+        newton_step_kernel<double><<<gb, 256, 0, c->stream>>>((double*)Gk, kk);
+      count_launch(c);
+      mm(m, kk, kk, U, m, OP_N, Gk, kk, OP_N, Y2, m, 1.0, 0.0);
+      NSG_CUDA(cudaMemcpyAsync(U, Y2, eb * m * kk, cudaMemcpyDeviceToDevice, c->stream));
+    }
+    return prev < 1e-13;
+  };
+  bool good = lowdin(kr);
+  if (good && kt > 0) {
+    void* W = U + eb * m * kr;
+    // project the tail off the resolved columns (twice), then orthonormalise it
+    for (int pass = 0; pass < 2; ++pass) {
+      mm(kr, kt, m, U, m, OP_C, W, m, OP_N, Gk, kr, 1.0, 0.0);
+      mm(m, kt, kr, U, m, OP_N, Gk, kr, OP_N, W, m, -1.0, 1.0);
+    }
+    void* Gt = dalloc(c, eb * kt * kt);
+    mm(kt, kt, m, W, m, OP_C, W, m, OP_N, Gt, kt, 1.0, 0.0);
+    void* E = dalloc(c, eb * kt * kt);
+    std::vector<double> wt;
+    PickFn all = [&](const std::vector<double>&, void** Z, int64_t* ldz) {
+      *Z = E;
+      *ldz = kt;
+      std::vector<int> cols(kt);
+      std::iota(cols.begin(), cols.end(), 0);
+      return cols;
+    };
+    try {
+      syevd_dc(c, dt, int(kt), Gt, wt, all);
+    } catch (...) {
+      dfree(c, Gt, eb * kt * kt);
+      dfree(c, E, eb * kt * kt);
+      dfree(c, Y2, eb * m * k);
+      dfree(c, Gk, eb * k * k);
+      free_tensor(c, Ut);
+      throw;
+    }
+    dfree(c, Gt, eb * kt * kt);
+    good = wt[0] > 1e-13 * wt[kt - 1] && wt[kt - 1] > 0.0;
+    if (good) {
+      std::vector<double> rs(kt);
+      for (int64_t i = 0; i < kt; ++i) rs[i] = 1.0 / std::sqrt(wt[i]);
+      DevBuf1 f(c, sizeof(double) * kt);
+      NSG_CUDA(cudaMemcpyAsync(f.p, rs.data(), sizeof(double) * kt, cudaMemcpyHostToDevice, c->stream));
+      void* F = Y2;  // E D^-1/2, then X = F E^H, then W X (scratch regions do not overlap)
+      NSG_CUDA(cudaMemcpyAsync(F, E, eb * kt * kt, cudaMemcpyDeviceToDevice, c->stream));
+      col_scale(F, kt, kt, (const double*)f.p);
+      mm(kt, kt, kt, F, kt, OP_N, E, kt, OP_C, Gk, kt, 1.0, 0.0);
+      mm(m, kt, kt, W, m, OP_N, Gk, kt, OP_N, Y2, m, 1.0, 0.0);
+      NSG_CUDA(cudaMemcpyAsync(W, Y2, eb * m * kt, cudaMemcpyDeviceToDevice, c->stream));
+      NSG_CUDA(cudaStreamSynchronize(c->stream));  // rs leaves scope
+      mm(kr, kt, m, U, m, OP_C, W, m, OP_N, Gk, kr, 1.0, 0.0);
+      mm(m, kt, kr, U, m, OP_N, Gk, kr, OP_N, W, m, -1.0, 1.0);
+      good = lowdin(k);
+    }
+    dfree(c, E, eb * kt * kt);
   }
+  dfree(c, Y2, eb * m * k);
   dfree(c, Gk, eb * k * k);
-  free_tensor(c, Y2);
   check_launch("factorize (tall)");
+  if (!good) {
+    free_tensor(c, Ut);
+    return false;
+  }
   // C = U^H M
   std::vector<int64_t> cdims;
   cdims.push_back(k);
   for (auto d : rdims) cdims.push_back(d);
   nsg_tensor* Ct = new_tensor(c, dt, int(cdims.size()), cdims.data(), false);
-  GemmArgs h = y;
-  h.M = k;
-  h.N = ncol;
-  h.K = m;
-  h.A = Ut->data;
-  h.lda = m;
-  h.opA = OP_C;
-  h.B = M->data;
-  h.ldb = m;
-  h.opB = OP_N;
-  h.C = Ct->data;
-  h.ldc = k;
-  h.alpha_re = sc;
-  gemm_accurate(c, h);
+  mm(k, ncol, m, Ut->data, m, OP_C, M->data, m, OP_N, Ct->data, k, sc, 0.0);
   *Uo = Ut;
   *Co = Ct;
   *ko = k;
@@ -337,13 +382,11 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
     }
     scale(c, dt, M->size, 1.0 / sc, 0.0, M->data);
   }
-  // The tall route is kept only when its smallest kept sigma^2 lies above 1e-11 of the
-  // largest (checked once the spectrum is known, before any eigenvector is formed).  A
-  // truncation that only the cutoff limits keeps weights down to ~cutoff / (discarded
-  // count) of the total, so with cutoff < 1e-10 and no maxdim below the narrow side the
-  // check fails on practically every spectrum: the attempt (Gram matrix, tridiagonal
-  // reduction and divide and conquer of the narrow side) is then skipped.
-  const bool tall_may_pass = cutoff >= 1e-10 || (maxdim > 0 && maxdim < ncol);
+  // The narrow side's Gram matrix is tried unless the call keeps everything (cutoff 0 and
+  // no maxdim below the narrow side, as a QR does): then the kept weights reach the Gram
+  // matrix's rounding, a rank-deficient M makes the route give up after its eigensolver,
+  // and M M^H is taken directly.
+  const bool tall_may_pass = cutoff > 0.0 || (maxdim > 0 && maxdim < ncol);
   if (ncol < m && ncol >= 16 && tall_may_pass) {
     std::vector<double> Pr;
     nsg_tensor *Ur = nullptr, *Cr = nullptr;

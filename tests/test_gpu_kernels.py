@@ -141,6 +141,47 @@ def test_factorize_truncation(nsg_ctx, cplx, m, n):
         assert abs(np.linalg.norm(M - Pk) ** 2 / np.linalg.norm(M) ** 2 - errref) < 1e-10
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("cplx", [False, True])
+@pytest.mark.parametrize("m,n,decay", [(600, 200, 0.88), (1500, 700, 0.965), (400, 100, 0.7)])
+def test_factorize_tall_unresolved_tail(nsg_ctx, cplx, m, n, decay, precision):
+    """Tall M whose kept spectrum reaches below what U = M V S^-1 resolves (kept sigma^2
+    down to ~1e-13 of the largest, 3 to 49 such columns): orthonormal U, exact bond
+    dimension (or one either side at a cutoff tie: the Gram matrix fixes partial sums of
+    the spectrum to ~eps sqrt(n) of the largest weight), discarded weight and
+    reconstruction.  Cutoffs far below that resolution (1e-15) leave the kept count itself
+    undetermined for any Gram-based factorization and are not used."""
+    rng = np.random.default_rng(m + n)
+    M = _spectrum_matrix(rng, m, n, decay, cplx)
+    l, r = Index(m), Index(n)
+    T = DTensor.from_numpy(M, [l, r])
+    s = np.linalg.svd(M, compute_uv=False)
+    for cutoff, maxdim in [(1e-12, None), (1e-13, n // 2), (3e-13, None)]:
+        nsg_ctx.set_precision(precision)
+        try:
+            U, Cc, info = it.factorize(T, [l], cutoff=cutoff, maxdim=maxdim, spectrum=True)
+        finally:
+            nsg_ctx.set_precision("fp64")
+        kref, errref = ol.truncate_spectrum(s ** 2, cutoff, maxdim)
+        if info["newdim"] != kref and _cutoff_tie(s ** 2, kref, cutoff, resolution=5e-14):
+            assert abs(info["newdim"] - kref) == 1
+            kref = info["newdim"]
+            errref = float((s ** 2)[kref:].sum() / (s ** 2).sum())
+        assert info["newdim"] == kref, (cutoff, maxdim)
+        u = U.to_numpy().reshape(m, -1)
+        assert np.abs(u.conj().T @ u - np.eye(kref)).max() < 1e-12
+        Pk = u @ Cc.to_numpy().reshape(kref, n)
+        assert abs(np.linalg.norm(M - Pk) ** 2 / np.linalg.norm(M) ** 2 - errref) < 1e-13
+        # a Gram matrix carries ~eps sqrt(n) sigma_max^2 of rounding, so a Gram-based
+        # factorization (either side, this library's or numpy's own) resolves kept singular
+        # values only to ~sqrt(eps sqrt(n)) sigma_max absolute; the part well above that is
+        # checked relatively
+        sp = np.linalg.svd(Pk, compute_uv=False)[:kref]
+        assert np.abs(sp - s[:kref]).max() < 4 * np.sqrt(np.finfo(float).eps * np.sqrt(n)) * s[0]
+        res = s[:kref] ** 2 > 1e-11 * s[0] ** 2
+        assert rel(sp[res], s[:kref][res]) < 1e-10
+
+
 def test_factorize_tensor_axes(nsg_ctx):
     rng = np.random.default_rng(5)
     a, s1, s2, b = Index(6), Index(2), Index(2), Index(5)
