@@ -166,6 +166,15 @@ int nsg_factorize(nsg_ctx* ctx, const nsg_tensor* T, const int* left_axes, int n
                   double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
                   nsg_tensor** C, int64_t* newdim, double* truncerr, double* spectrum,
                   int64_t spectrum_cap);
+/* nsg_factorize (no spectrum) that also returns, in *Uperp, an orthonormal basis
+ * [left dims..., rows - k] of the complement of U's columns in the row space when the
+ * factorization went through the row-side Gram matrix M M^H (the discarded
+ * eigenvectors), NULL otherwise (the narrow-side route for tall M, or k = rows).  The
+ * densitymatrix expansion of the next region (subspace/densitymatrix.jl:44-59) works in
+ * this complement: its eigen(rho) restricted to it is the same eigenproblem. */
+int nsg_factorize_complement(nsg_ctx* ctx, const nsg_tensor* T, const int* left_axes, int n_left,
+                             double cutoff, int64_t maxdim, int64_t mindim, nsg_tensor** U,
+                             nsg_tensor** C, nsg_tensor** Uperp, int64_t* newdim, double* truncerr);
 /* Q: [left dims..., k], R: [k, right dims...], k = min(rows, cols). */
 int nsg_qr(nsg_ctx* ctx, const nsg_tensor* T, const int* left_axes, int n_left,
            nsg_tensor** Q, nsg_tensor** R);

@@ -356,10 +356,11 @@ static bool factorize_right(nsg_ctx* c, nsg_tensor* M, int64_t m, int64_t ncol, 
 
 static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, double cutoff,
                           int64_t maxdim, int64_t mindim, nsg_tensor** U, nsg_tensor** C, int64_t* newdim,
-                          double* truncerr, double* spectrum, int64_t spectrum_cap) {
+                          double* truncerr, double* spectrum, int64_t spectrum_cap, nsg_tensor** Uperp = nullptr) {
   NSG_API_BEGIN(c)
   NSG_CHECK(c && T && U && C, NSG_ERR_INVALID, "null argument");
   NSG_CHECK(n_left >= 1 && n_left < T->rank, NSG_ERR_INVALID, "factorize: need left and right axes");
+  if (Uperp) *Uperp = nullptr;
   int64_t m, ncol;
   std::vector<int64_t> ldims, rdims;
   bool owned = false;
@@ -436,6 +437,10 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   nsg_tensor* Ut = nullptr;
   std::vector<double> P;
   std::vector<double> w;
+  // with Uperp requested, every eigenvector is back-transformed (kept ones first): the
+  // discarded ones are an orthonormal basis of the complement of U's columns
+  void* Zall = nullptr;
+  size_t zbytes = 0;
   PickFn pick = [&](const std::vector<double>& wa, void** Z, int64_t* ldz) {
     // descending spectrum
     P.assign(wa.rbegin(), wa.rend());
@@ -443,10 +448,15 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
     std::vector<int64_t> udims = ldims;
     udims.push_back(k);
     Ut = new_tensor(c, dt, int(udims.size()), udims.data(), false);
-    *Z = Ut->data;
+    const int64_t ncols = (Uperp && k < m) ? m : k;
+    if (ncols > k) {
+      zbytes = eb * size_t(m) * size_t(m);
+      Zall = dalloc(c, zbytes);
+    }
+    *Z = Zall ? Zall : Ut->data;
     *ldz = m;
-    std::vector<int> cols(k);
-    for (int64_t i = 0; i < k; ++i) cols[i] = int(m - 1 - i);
+    std::vector<int> cols(ncols);
+    for (int64_t i = 0; i < ncols; ++i) cols[i] = int(m - 1 - i);
     return cols;
   };
   try {
@@ -454,10 +464,21 @@ static int factorize_impl(nsg_ctx* c, const nsg_tensor* T, const int* left_axes,
   } catch (...) {
     dfree(c, G, eb * m * m);
     if (Ut) free_tensor(c, Ut);
+    if (Zall) dfree(c, Zall, zbytes);
     if (owned) free_tensor(c, M);
     throw;
   }
   dfree(c, G, eb * m * m);
+  if (Zall) {
+    std::vector<int64_t> pdims = ldims;
+    pdims.push_back(m - k);
+    nsg_tensor* Qp = new_tensor(c, dt, int(pdims.size()), pdims.data(), false);
+    NSG_CUDA(cudaMemcpyAsync(Ut->data, Zall, eb * size_t(m) * size_t(k), cudaMemcpyDeviceToDevice, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(Qp->data, (char*)Zall + eb * size_t(m) * size_t(k), eb * size_t(m) * size_t(m - k),
+                             cudaMemcpyDeviceToDevice, c->stream));
+    dfree(c, Zall, zbytes);
+    *Uperp = Qp;
+  }
   // C = U^H M
   std::vector<int64_t> cdims;
   cdims.push_back(k);
@@ -498,6 +519,14 @@ int nsg_factorize(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_l
                   double* spectrum, int64_t spectrum_cap) {
   return factorize_impl(c, T, left_axes, n_left, cutoff, maxdim, mindim, U, C, newdim, truncerr, spectrum,
                         spectrum_cap);
+}
+
+int nsg_factorize_complement(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, double cutoff,
+                             int64_t maxdim, int64_t mindim, nsg_tensor** U, nsg_tensor** C, nsg_tensor** Uperp,
+                             int64_t* newdim, double* truncerr) {
+  if (!Uperp) return factorize_impl(c, T, left_axes, n_left, cutoff, maxdim, mindim, U, C, newdim, truncerr,
+                                    nullptr, 0);
+  return factorize_impl(c, T, left_axes, n_left, cutoff, maxdim, mindim, U, C, newdim, truncerr, nullptr, 0, Uperp);
 }
 
 int nsg_qr(nsg_ctx* c, const nsg_tensor* T, const int* left_axes, int n_left, nsg_tensor** Q, nsg_tensor** R) {

@@ -273,9 +273,12 @@ def _axes(t, inds):
     return [t.inds.index(i) for i in inds]
 
 
-def factorize(T: DTensor, left, cutoff=0.0, maxdim=None, mindim=1, tags="Link", spectrum=False):
+def factorize(T: DTensor, left, cutoff=0.0, maxdim=None, mindim=1, tags="Link", spectrum=False, complement=False):
     """ITensors `factorize(T, left; ortho="left", cutoff, maxdim, mindim)` on device.
-    Returns (U, C, info) with U[left..., link], C[link, right...]."""
+    Returns (U, C, info) with U[left..., link], C[link, right...].  With complement=True
+    (and spectrum=False), info["complement"] is an orthonormal basis Uperp[left..., perp] of
+    the complement of U's columns when the factorization produced one
+    (nsg_factorize_complement), else None."""
     T = T.materialize()
     ctx = T.ctx
     left = [i for i in T.inds if i in left]
@@ -283,18 +286,30 @@ def factorize(T: DTensor, left, cutoff=0.0, maxdim=None, mindim=1, tags="Link", 
     ax = (C.c_int * len(left))(*_axes(T, left))
     U, Cc = C.c_void_p(), C.c_void_p()
     k, err = C.c_int64(), C.c_double()
-    cap = int(min(np.prod([i.dim for i in left]), np.prod([i.dim for i in right])))
-    spec = (C.c_double * cap)() if spectrum else None
     md = -1 if maxdim is None else int(maxdim)
-    ctx.check(ctx.L.nsg_factorize(ctx.h, T.st.h, ax, len(left), float(cutoff), md, int(mindim),
-                                  C.byref(U), C.byref(Cc), C.byref(k), C.byref(err), spec,
-                                  cap if spectrum else 0))
+    perp = None
+    if complement and not spectrum:
+        Up = C.c_void_p()
+        ctx.check(ctx.L.nsg_factorize_complement(ctx.h, T.st.h, ax, len(left), float(cutoff), md, int(mindim),
+                                                 C.byref(U), C.byref(Cc), C.byref(Up), C.byref(k), C.byref(err)))
+        if Up.value:
+            rows = int(np.prod([i.dim for i in left]))
+            perp = DTensor(Storage(ctx, Up, T.dtype, [i.dim for i in left] + [rows - k.value]),
+                           left + [Index(rows - k.value, "Link,perp")])
+    else:
+        cap = int(min(np.prod([i.dim for i in left]), np.prod([i.dim for i in right])))
+        spec = (C.c_double * cap)() if spectrum else None
+        ctx.check(ctx.L.nsg_factorize(ctx.h, T.st.h, ax, len(left), float(cutoff), md, int(mindim),
+                                      C.byref(U), C.byref(Cc), C.byref(k), C.byref(err), spec,
+                                      cap if spectrum else 0))
     link = Index(k.value, tags)
     Ut = DTensor(Storage(ctx, U, T.dtype, [i.dim for i in left] + [k.value]), left + [link])
     Ct = DTensor(Storage(ctx, Cc, T.dtype, [k.value] + [i.dim for i in right]), [link] + right)
     info = dict(truncerr=err.value, newdim=k.value)
     if spectrum:
         info["spectrum"] = np.array(spec[: k.value])
+    if complement:
+        info["complement"] = perp
     return Ut, Ct, info
 
 

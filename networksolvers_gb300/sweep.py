@@ -169,6 +169,14 @@ def subspace_expand(problem, local, region_iterator, algorithm, trunc, expansion
     if expand <= 0:
         return problem, local
     tr = dict(trunc, maxdim=expand)
+    # An orthonormal complement of A's columns, when the factorization that made A produced
+    # one (its discarded eigenvectors; the inserter keeps the latest once an expansion has
+    # run): eigen(rho) restricted to it is the same eigenproblem, of dimension
+    # rows(A) - dim(a) instead of rows(A), since rho = X X^H with X = (1 - A A^H) sqrt_rho.
+    basis = getattr(problem, "expansion_basis", None)
+    if basis is None:
+        problem.expansion_basis = basis = ()
+    perp = basis[2] if (basis and basis[0] == pv and basis[1] is A.st and not A.conj) else None
     # the expansion's projections are checked against a 1e-10 orthogonality guard
     # (densitymatrix.jl:59): its contractions run at FP64 accuracy whatever the context's
     # mode (eight-slice tensor-core products in the split form, FP64 cores otherwise)
@@ -176,12 +184,12 @@ def subspace_expand(problem, local, region_iterator, algorithm, trunc, expansion
     prec = ctx.precision
     ctx.set_precision("ozaki8" if prec in ("ozaki", "ozaki8") else "fp64")
     try:
-        return _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass)
+        return _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass, perp)
     finally:
         ctx.set_precision(prec)
 
 
-def _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass):
+def _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass, perp=None):
     parts = [A]
     for (u, v) in P.incident_edges(P.pos):
         if u in region or v in region:
@@ -190,12 +198,21 @@ def _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_p
     parts.append(P.H[pv])
     from .itensors import contract
     sqrt_rho = contract(parts)
-    Ap = A.prime()
-    for _ in range(north_pass):
-        sqrt_rho = sqrt_rho - Ap * (Ap.dag() * sqrt_rho)
-    rho = sqrt_rho * sqrt_rho.noprime().dag()
     ket = uniqueinds(A, Cn)
-    D, U, u = eigen_hermitian(rho, ket, **tr)
+    if perp is not None and {i.key() for i in perp.inds[:-1]} == {i.key() for i in ket}:
+        # Y = Uperp^H sqrt_rho (Uperp^H A = 0 makes the projection redundant), R = Y Y^H,
+        # eigenvectors Uperp Z
+        q = perp.inds[-1]
+        Y = perp.prime().dag() * sqrt_rho
+        R = Y * Y.noprime().dag()
+        D, Z, u = eigen_hermitian(R, [q], **tr)
+        U = perp * Z
+    else:
+        Ap = A.prime()
+        for _ in range(north_pass):
+            sqrt_rho = sqrt_rho - Ap * (Ap.dag() * sqrt_rho)
+        rho = sqrt_rho * sqrt_rho.noprime().dag()
+        D, U, u = eigen_hermitian(rho, ket, **tr)
     Apa = A.prime(a)
     for _ in range(north_pass):
         U = U - Apa * (Apa.dag() * U)
@@ -247,8 +264,14 @@ def inserter(problem, local, region_iterator, sweep, normalize=False, set_orthog
     if len(region) == 1:
         Cn = local
     elif len(region) == 2:
-        U, Cn, info = factorize(local, list(psi[region[0]].inds), **trunc)
+        # once a densitymatrix expansion has run, keep the complement of U's columns for the
+        # next region's expansion of this vertex
+        basis = getattr(problem, "expansion_basis", None)
+        U, Cn, info = factorize(local, list(psi[region[0]].inds), complement=basis is not None, **trunc)
         psi[region[0]] = U
+        if basis is not None:
+            perp = info.pop("complement", None)
+            problem.expansion_basis = (region[0], U.st, perp) if perp is not None else ()
     else:
         raise ValueError(f"Region of length {len(region)} not currently supported")
     v = region[-1]
