@@ -286,9 +286,11 @@ def run_nsg(args):
         if dom == "tridiag":
             # DRAM bytes of one launch from the ncu capture at n = 1024 (8.44 MB read + 1.83 MB
             # written: the L2-resident matrix once, the reflectors back), scaled by n^2 to the
-            # n = 2048 launches of the bond-dimension-1024 regions
-            roof["traffic"] = 10.27e6 * 4.0
-            roof["traffic_note"] = "bytes per n=2048 launch, scaled from ncu at n=1024 (n^2)"
+            # launches' mean order, which the algorithmic flops per launch (4/3 n^3) give
+            n_eff = (0.75 * c["flops"] / c["launches"]) ** (1.0 / 3.0)
+            roof["traffic"] = 10.27e6 * (n_eff / 1024.0) ** 2
+            roof["traffic_note"] = (f"bytes per launch at the launches' mean order n = {n_eff:.0f} (from 4/3 n^3 "
+                                    f"flops per launch), scaled by n^2 from ncu at n=1024")
     tc = classes.get("tc_gemm")
     heff_tflops = (tc["flops"] / (tc["ms"] / 1e3) / 1e12) if tc else None
     cpu = None
