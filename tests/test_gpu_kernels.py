@@ -211,6 +211,53 @@ def test_eigh_truncated(nsg_ctx, cplx):
     assert rel(M @ Um, Um * D) < 1e-10
 
 
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+@pytest.mark.parametrize("cplx", [False, True])
+def test_factorize_complement_and_reduced_expansion(nsg_ctx, cplx, precision):
+    """nsg_factorize_complement: Uperp [left..., rows - k] orthonormal and orthogonal to U,
+    U and C as nsg_factorize gives them, none from the narrow-side route; and the
+    densitymatrix eigenproblem solved in Uperp (R = Y Y^H, Y = Uperp^H sqrt_rho) gives the
+    eigenvalues and the eigenvector subspace of the full rho = X X^H, X = (1 - U U^H) sqrt_rho."""
+    rng = np.random.default_rng(21)
+    a, s, b = Index(40), Index(2), Index(96)
+    M = _dmrg_like(rng, 80, 96, cplx).reshape(40, 2, 96)
+    T = DTensor.from_numpy(M, [a, s, b])
+    nsg_ctx.set_precision(precision)
+    try:
+        U, Cc, info = it.factorize(T, [a, s], cutoff=1e-10, maxdim=50, complement=True)
+        U0, C0, info0 = it.factorize(T, [a, s], cutoff=1e-10, maxdim=50)
+        perp = info["complement"]
+        k = info["newdim"]
+        assert perp is not None and list(perp.inds[:2]) == [a, s] and perp.inds[2].dim == 80 - k
+        u, q = U.to_numpy().reshape(80, k), perp.to_numpy().reshape(80, 80 - k)
+        assert np.abs(q.conj().T @ q - np.eye(80 - k)).max() < 1e-12
+        assert np.abs(u.conj().T @ q).max() < 1e-12
+        assert info0["newdim"] == k and rel(u, U0.to_numpy().reshape(80, k)) < 1e-12
+        assert rel(Cc.to_numpy(), C0.to_numpy()) < 1e-12
+        # reduced expansion against the full one
+        w_, o = Index(3), Index(30)
+        S = rnd(rng, (40, 2, 3, 30), cplx)
+        sq = DTensor.from_numpy(S, [a.prime(), s.prime(), w_, o])
+        Y = perp.prime().dag() * sq
+        R = Y * Y.noprime().dag()
+        D, Z, _ = it.eigen_hermitian(R, [perp.inds[2]], cutoff=1e-14, maxdim=20)
+        Ue = (perp * Z).to_numpy().reshape(80, -1)
+        X = S.reshape(80, 90)
+        X = X - u @ (u.conj().T @ X)
+        wf, Vf = np.linalg.eigh(X @ X.conj().T)
+        wf, Vf = wf[::-1][: len(D)], Vf[:, ::-1][:, : len(D)]
+        assert rel(np.array(D), wf) < 1e-12
+        # same subspace: the projector difference
+        assert np.abs(Ue @ Ue.conj().T - Vf @ Vf.conj().T).max() < 1e-10
+        # the narrow-side route (tall M, cutoff > 0) returns no complement
+        Mt = _dmrg_like(rng, 200, 40, cplx)
+        lt, rt = Index(200), Index(40)
+        _, _, it_info = it.factorize(DTensor.from_numpy(Mt, [lt, rt]), [lt], cutoff=1e-12, complement=True)
+        assert it_info["complement"] is None
+    finally:
+        nsg_ctx.set_precision("fp64")
+
+
 def _chain_heff(rng, chi_l, chi_r, w=5, d=2, cplx=False):
     """A Hermitian 2-site H_eff: L, W1, W2, R hermitised so that the map is Hermitian."""
     def herm_env(chi):
