@@ -8,12 +8,12 @@ One step = one full sweep (198 two-site regions).  Warm-up steps are the first W
 of the schedule, the timed steps the next K sweeps.  Metric: sweeps/s (higher is
 better); the split-precision form is the product path: the large contractions (H_eff,
 environments) run as six-slice BF16 products with exact FP32 chunk accumulation on
-tcgen05, the eigensolver's GEMMs, `C = U^H M` and the density-matrix expansion as
-eight-slice products (FP64 accuracy), while the Gram matrices, the tridiagonalisation,
-the secular equations and the Lanczos scalars stay FP64; `--precision tf32x3` is the
-three-product TF32 form and `--precision fp64` the plain form (every contraction on the
-FP64 CUDA cores).  Other workloads (`--workload c1|tdvp|batch|serve|accuracy`) print
-their own lines; see `main()`.
+tcgen05, the factorization's Gram matrices, the eigensolver's GEMMs, `C = U^H M` and the
+density-matrix expansion as eight-slice products (FP64 accuracy), while the
+tridiagonalisation, the secular equations and the Lanczos scalars stay FP64;
+`--precision tf32x3` is the three-product TF32 form and `--precision fp64` the plain form
+(every contraction on the FP64 CUDA cores).  Other workloads
+(`--workload c1|tdvp|batch|serve|accuracy|qn`) print their own lines; see `main()`.
 
 Timing: CUDA events on the library's stream around each timed sweep; the per-kernel
 roofline comes from events around each launch of the dominant kernel classes in the
@@ -574,6 +574,65 @@ def run_serve(args):
           max_rel_dE_vs_sequential=max(same) if same else None)
 
 
+def run_qn(args):
+    """U(1) block-sparse DMRG (the `conserve_qns=true` path): Heisenberg chain N=40 from the
+    Neel state, 2-site, maxdim [32, 64, 128, 256] then 256, cutoff 1e-10, Lanczos krylovdim
+    3 / maxiter 1; one step = one sweep (W warm-up sweeps, K timed, host clock around
+    synchronised sweeps).  Beside it: the dense GPU chain driver on the same run, and the
+    dense CPU oracle on its sweeps 1..W+1 (sample)."""
+    import networksolvers_gb300.models as m
+    from networksolvers_gb300 import _native, qn
+    from networksolvers_gb300.chain import dmrg_chain
+    ctx = _native.Context(0, precision=args.precision)
+    _native.set_default_context(ctx)
+    n = 40
+    H = m.heisenberg_chain(n)
+    g = m.chain_graph(n)
+    states = [0 if v % 2 else 1 for v in range(1, n + 1)]
+    psi0 = m.product_state(g, {v: ("Up" if v % 2 else "Dn") for v in g.vertices})
+    total = args.warmup + args.steps
+    kw = dict(maxdim=[32, 64, 128, 256], cutoff=1e-10, krylovdim=3, maxiter=1)
+    nreg = 2 * (n - 1)
+
+    def timed(run):
+        marks = []
+
+        def cb(sweep, k, energy, info):
+            if k == nreg - 1:
+                ctx.synchronize()
+                marks.append(time.perf_counter())
+
+        ctx.synchronize()
+        t0 = time.perf_counter()
+        out = run(cb)
+        marks = [t0] + marks
+        return out, marks[total] - marks[args.warmup]
+
+    (Eq, A, rq), tq = timed(lambda cb: qn.qn_dmrg_chain(H, states, total, ctx=ctx, region_callback=cb, **kw))
+    (Ed, _, rd), td = timed(lambda cb: dmrg_chain(H, psi0, total, ctx=ctx, region_callback=cb, **kw))
+    nnz = sum(t.nnz() for t in A)
+    dense_size = sum(int(np.prod([q.dim for q in t.inds])) for t in A)
+    cpu = None
+    if not args.no_cpu:
+        from oracle import sweep as osw
+        okw = dict(nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+                   inserter_kwargs=dict(trunc=dict(cutoff=1e-10, maxdim=kw["maxdim"])))
+        sample = args.warmup + 1
+        tc = _oracle_sweep_seconds(lambda cbk: osw.dmrg(H, psi0, nsweeps=sample, sweep_callback=cbk, **okw),
+                                   sample, 1)
+        cpu = {"value": 1.0 / tc, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"dense oracle, sweep {sample} of the same schedule"}
+    _line(metric="qn_dmrg_sweeps_per_s", value=args.steps / tq, unit="sweeps/s", steps=args.steps,
+          warmup=args.warmup, ms_per_step=tq * 1e3 / args.steps,
+          dtype="f64" if args.precision == "fp64" else f"{args.precision}+f64",
+          config={"workload": "heisenberg_chain_N40_2site_qn_dmrg_maxdim256", "start": "Neel", "cutoff": 1e-10,
+                  "timing": "host clock around synchronised sweeps"},
+          energy=Eq, dense_gpu={"value": args.steps / td, "unit": "sweeps/s", "energy": Ed,
+                                "rel_dE": abs(Eq - Ed) / abs(Ed),
+                                "bond_dims_equal": [r[3] for r in rq] == [r[3] for r in rd]},
+          block_sparse_fraction=nnz / dense_size, maxlinkdim=max(r[3] for r in rq), cpu_baseline=cpu)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -583,9 +642,10 @@ def main():
     ap.add_argument("--precision", default="ozaki", choices=["ozaki", "tf32x3", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve", "accuracy"],
+    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve", "accuracy", "qn"],
                     help="dmrg: the N=100 benchmark (default); c1: the N=20 chain; tdvp: binary-tree TFIM "
-                         "TDVP; batch: 256 J1-J2 chains on a solve pool; serve: Poisson request stream")
+                         "TDVP; batch: 256 J1-J2 chains on a solve pool; serve: Poisson request stream; "
+                         "qn: U(1) block-sparse DMRG")
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--sample", type=int, default=16)
@@ -594,7 +654,7 @@ def main():
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--sweeps", type=int, default=10)
     args = ap.parse_args()
-    if args.warmup < 3 and args.workload in ("dmrg", "c1", "tdvp"):
+    if args.warmup < 3 and args.workload in ("dmrg", "c1", "tdvp", "qn"):
         raise SystemExit("warmup must be >= 3")
     if args.impl == "reference":
         run_reference(args)
@@ -608,6 +668,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "qn":
+        run_qn(args)
     else:
         run_nsg(args)
 

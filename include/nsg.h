@@ -123,6 +123,14 @@ int nsg_norm(nsg_ctx* ctx, const nsg_tensor* x, double* out);
 int nsg_permute(nsg_ctx* ctx, const nsg_tensor* x, const int* perm, int conj, nsg_tensor** out);
 /* concatenate along `axis` (all other dims equal)  — ITensors directsum */
 int nsg_concat(nsg_ctx* ctx, const nsg_tensor* a, const nsg_tensor* b, int axis, nsg_tensor** out);
+/* dst(r0d + i, c0d + j) = src(r0s + i, c0s + j) (accumulate != 0: +=) for i < rows, j < cols,
+ * each tensor's column-major storage viewed as a matrix with leading dimension lds / ldd;
+ * the boxes must lie inside both tensors.  The block-sparse (QN) layer assembles the
+ * sector matrices of its factorizations and cuts its blocks back out with it (NDTensors
+ * BlockSparse storage: per-block dense data placed at block offsets). */
+int nsg_copy_submatrix(nsg_ctx* ctx, const nsg_tensor* src, int64_t lds, int64_t r0s, int64_t c0s,
+                       nsg_tensor* dst, int64_t ldd, int64_t r0d, int64_t c0d, int64_t rows, int64_t cols,
+                       int accumulate);
 
 /* ---- contraction ---------------------------------------------------------
  * Contract n tensors; tensor k has rank r_k (its own rank) and labels

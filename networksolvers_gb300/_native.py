@@ -74,6 +74,7 @@ _SIGS = {
     "nsg_factorize": (i32, [p, p, P_int, i32, dbl, i64, i64, P_p, P_p, P_i64, P_dbl, P_dbl, i64]),
     "nsg_factorize_complement": (i32, [p, p, P_int, i32, dbl, i64, i64, P_p, P_p, P_p, P_i64, P_dbl]),
     "nsg_qr": (i32, [p, p, P_int, i32, P_p, P_p]),
+    "nsg_copy_submatrix": (i32, [p, p, i64, i64, i64, p, i64, i64, i64, i64, i64, i32]),
     "nsg_eigh": (i32, [p, p, P_int, i32, dbl, i64, i64, P_p, P_dbl, i64, P_i64, P_dbl]),
     "nsg_gemm_tf32x3_noalloc": (i32, [p, i64, i32, p, i64, i32, p, i64, i64, i64, i64, dbl, dbl, p,
                                       C.c_char_p, i32]),

@@ -435,6 +435,66 @@ void row_norms2(nsg_ctx* c, int dtype, int64_t rows, int64_t cols, const void* A
 
 using namespace nsg;
 
+// dst(r0d + i, c0d + j) (+)= src(r0s + i, c0s + j) for i < rows, j < cols, both tensors
+// viewed as column-major matrices with the given leading dimensions
+template <typename T, bool ACC>
+__global__ void copy_submatrix_kernel(const T* __restrict__ src, int64_t lds, T* __restrict__ dst, int64_t ldd,
+                                      int64_t rows, int64_t cols) {
+  const int64_t tot = rows * cols;
+  for (int64_t e = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; e < tot; e += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t i = e % rows, j = e / rows;
+    const T v = src[i + j * lds];
+    if constexpr (ACC) {
+      if constexpr (sizeof(T) == 8) {
+        dst[i + j * ldd] += v;
+      } else {
+        T& d = dst[i + j * ldd];
+        d.x += v.x;
+        d.y += v.y;
+      }
+    } else {
+      dst[i + j * ldd] = v;
+    }
+  }
+}
+
+extern "C" int nsg_copy_submatrix(nsg_ctx* c, const nsg_tensor* src, int64_t lds, int64_t r0s, int64_t c0s,
+                                  nsg_tensor* dst, int64_t ldd, int64_t r0d, int64_t c0d, int64_t rows, int64_t cols,
+                                  int accumulate) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && src && dst, NSG_ERR_INVALID, "null argument");
+  NSG_CHECK(src->dtype == dst->dtype, NSG_ERR_INVALID, "copy_submatrix: dtypes differ");
+  NSG_CHECK(rows >= 0 && cols >= 0 && lds >= 1 && ldd >= 1 && r0s >= 0 && c0s >= 0 && r0d >= 0 && c0d >= 0,
+            NSG_ERR_INVALID, "copy_submatrix: negative extent or offset");
+  if (rows == 0 || cols == 0) return NSG_OK;
+  NSG_CHECK(r0s + rows <= lds && r0d + rows <= ldd, NSG_ERR_INVALID, "copy_submatrix: rows beyond the leading dimension");
+  NSG_CHECK(r0s + rows + (c0s + cols - 1) * lds <= src->size, NSG_ERR_INVALID, "copy_submatrix: box beyond the source");
+  NSG_CHECK(r0d + rows + (c0d + cols - 1) * ldd <= dst->size, NSG_ERR_INVALID,
+            "copy_submatrix: box beyond the destination");
+  const int grid = grid_for(c, rows * cols);
+  const size_t eb = elem_bytes(src->dtype);
+  const char* s = (const char*)src->data + eb * size_t(r0s + c0s * lds);
+  char* d = (char*)dst->data + eb * size_t(r0d + c0d * ldd);
+  if (src->dtype == NSG_C128) {
+    if (accumulate)
+      copy_submatrix_kernel<double2, true><<<grid, kThreads, 0, c->stream>>>((const double2*)s, lds, (double2*)d, ldd,
+                                                                           rows, cols);
+    else
+      copy_submatrix_kernel<double2, false><<<grid, kThreads, 0, c->stream>>>((const double2*)s, lds, (double2*)d,
+                                                                            ldd, rows, cols);
+  } else {
+    if (accumulate)
+      copy_submatrix_kernel<double, true><<<grid, kThreads, 0, c->stream>>>((const double*)s, lds, (double*)d, ldd,
+                                                                          rows, cols);
+    else
+      copy_submatrix_kernel<double, false><<<grid, kThreads, 0, c->stream>>>((const double*)s, lds, (double*)d, ldd,
+                                                                           rows, cols);
+  }
+  count_launch(c);
+  check_launch("copy_submatrix");
+  NSG_API_END(c)
+}
+
 extern "C" int nsg_concat(nsg_ctx* c, const nsg_tensor* a, const nsg_tensor* b, int axis, nsg_tensor** out) {
   NSG_API_BEGIN(c)
   NSG_CHECK(c && a && b && out, NSG_ERR_INVALID, "null argument");
