@@ -211,6 +211,10 @@ def run_nsg(args):
     for sweep in range(1, total + 1):
         timed = sweep > args.warmup
         if timed and sweep == args.warmup + 1:
+            if rank == 0 and not args.no_e2e:
+                # host copy of the state entering the timed sweeps (outside the timed region):
+                # the e2e leg replays the same sweeps from it through the public API
+                snap = (prob.state.to_numpy(psi0), list(prob.state.ortho_region))
             if dist:
                 td.barrier()
             ctx.synchronize()
@@ -241,24 +245,25 @@ def run_nsg(args):
     clk = clocks.stop()
     t_sweep = replica_time(float(np.sum(sweep_ms)) / 1e3, device="cuda" if dist else None)
     value = replica_throughput(world, args.steps, t_sweep)
-    # e2e: one sweep through the public API from host buffers (upload, sweep, download)
+    # e2e: the timed sweeps again through the public API from host buffers, one `dmrg`
+    # call per sweep (upload of the state and the operator, environments built from
+    # scratch, the sweep, download of the state), from the host copy taken before them
     e2e = None
     if rank == 0 and not args.no_e2e:
-        arrays = prob.state.to_numpy(psi0)
         from networksolvers_gb300.models import Network
-        # the host copy keeps the state's gauge (its orthogonality centre), as a TTN does
-        host_state = Network(psi0.graph, arrays, psi0.legs, np.float64,
-                             {"kind": "state", "ortho_region": list(prob.state.ortho_region)})
-        h2d = sum(a.nbytes for a in arrays.values()) + sum(t.nbytes for t in H.tensors.values())
-        off = min(args.warmup + args.steps, len(SCHEDULE)) - 1
-        kw2 = kwargs_for(off)
+        arrays, ortho = snap
+        h2d = d2h = 0
         t0 = time.perf_counter()
-        E2, psi2 = ns.dmrg(H, host_state, nsweeps=1, **kw2)
-        out = psi2.to_numpy(psi0)
+        for k in range(args.steps):
+            # the host copy keeps the state's gauge (its orthogonality centre), as a TTN does
+            host_state = Network(psi0.graph, arrays, psi0.legs, np.float64, {"kind": "state", "ortho_region": ortho})
+            h2d += sum(a.nbytes for a in arrays.values()) + sum(t.nbytes for t in H.tensors.values())
+            E2, psi2 = ns.dmrg(H, host_state, nsweeps=1, **kwargs_for(args.warmup + k))
+            arrays, ortho = psi2.to_numpy(psi0), list(psi2.ortho_region)
+            d2h += sum(a.nbytes for a in arrays.values()) + 8
         t1 = time.perf_counter()
-        d2h = sum(a.nbytes for a in out.values()) + 8
-        e2e = {"value": 1.0 / (t1 - t0), "unit": "sweeps/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
+        e2e = {"value": args.steps / (t1 - t0), "unit": "sweeps/s", "h2d_bytes_per_step": int(h2d // args.steps),
+               "d2h_bytes_per_step": int(d2h // args.steps), "energy": E2}
     bf16, hbm, kind = peaks()
     # roofline of the dominant kernel class in the timed region
     classes = {k: v for k, v in prof.items() if v["launches"] > 0}
