@@ -42,7 +42,7 @@ _qn_ids = itertools.count(1)
 class QNIndex:
     """An index with U(1) sectors ((qn, dim), ...) and a direction (+1 / -1)."""
 
-    __slots__ = ("sectors", "dir", "tags", "plev", "id", "dim", "offsets")
+    __slots__ = ("sectors", "dir", "tags", "plev", "id", "dim", "offsets", "_sec")
 
     def __init__(self, sectors, dir=1, tags="", plev=0, id=None):
         self.sectors = tuple((int(q), int(d)) for q, d in sectors)
@@ -56,6 +56,7 @@ class QNIndex:
             offs.append(o)
             o += d
         self.offsets = tuple(offs)
+        self._sec = {}
 
     def prime(self, n=1):
         return QNIndex(self.sectors, self.dir, self.tags, self.plev + n, self.id)
@@ -80,7 +81,10 @@ class QNIndex:
 
     def sec(self, s):
         """The dense index of sector s (the label the device contraction sees)."""
-        return Index(self.sectors[s][1], self.tags, self.plev, (self.id, s))
+        ix = self._sec.get(s)
+        if ix is None:
+            ix = self._sec[s] = Index(self.sectors[s][1], self.tags, self.plev, (self.id, s))
+        return ix
 
     def __repr__(self):
         return f"QNIndex({list(self.sectors)},dir={self.dir},id={self.id}{chr(39) * self.plev})"
@@ -263,6 +267,8 @@ def qfactorize(t: BlockTensor, left, cutoff=0.0, maxdim=None, mindim=1, tags="Li
     (rows x cols) matrix is assembled on the device and factorized there (all its
     singular values kept), the truncation runs over all sectors' values together, and
     U [left..., link (-1)], C [link (+1), right...] are cut back into blocks."""
+    if not t.blocks:
+        raise ValueError("qfactorize: the tensor has no blocks (it is zero)")
     ctx = next(iter(t.blocks.values())).ctx
     lp = [t.inds.index(q) for q in left]
     rp = [i for i in range(len(t.inds)) if i not in lp]
