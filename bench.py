@@ -42,6 +42,12 @@ CUTOFF = 1e-12
 REGIONS_PER_SWEEP = 2 * (N_SITES - 1)
 
 
+# GB300 FP64 rate: the measured peaks hold no FP64 figure; kernelbench's FP64 GEMM at
+# 4096^3 reaches 1.25 TFLOP/s (cuBLAS DGEMM 1.10) on these GPUs, the nominal figure
+FP64_PEAK_TFLOPS = 1.25
+FP64_PEAK_NOTE = "GB300 FP64 rate (no FP64 figure in the measured peaks; 1.25 TFLOP/s nominal)"
+
+
 def peaks():
     f = ROOT / "MEASURED_PEAKS.json"
     if f.exists():
@@ -122,62 +128,131 @@ def kwargs_for(sweep_offset=0):
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the oracle on a bounded steady-state sample (one region step at
-# bond dimension 1024: 3 H_eff applications in Lanczos, truncated SVD, environment update)
+# CPU baseline: the oracle (the reference's sweep restated on FP64 numpy/OpenBLAS)
+# running real region steps of the workload's sweep, one region per step
 # ---------------------------------------------------------------------------
 
+# Largest bond dimension of each sweep of this workload's 10-sweep schedule and beyond,
+# as the split-precision GPU run reaches them (the bond dimension saturates near 475 once
+# the cutoff 1e-12 governs the truncation); the reference arm samples region steps at
+# these sizes, the GPU arm passes the sizes it actually reached.
+SWEEP_BOND = {1: 64, 2: 128, 3: 256, 4: 512, 5: 1024, 6: 1024, 7: 1024, 8: 1024, 9: 863, 10: 600}
+CONVERGED_BOND = 475
 
-def cpu_region_sample(nregions=2, chi=1024, seed=7):
-    from oracle import krylov as ok, linalg as ol
-    from oracle.tensor import Index, Tensor
+
+def sweep_bond(sweep):
+    return SWEEP_BOND.get(sweep, CONVERGED_BOND)
+
+
+def cpu_region_step(sweep, position, cap, seed):
+    """Seconds the oracle takes for region `position` (0..197) of sweep `sweep` of the
+    workload: the complete reference region step (extracter with the densitymatrix
+    expansion, Lanczos with 3 H_eff applications, truncated factorization; iterators.jl:
+    81-100) on all host threads.  The state is a seeded random MPS in the gauge the sweep
+    has at that region (orthogonality centre on the region's first vertex) with bond
+    dimensions min(2^i, 2^(N-i), cap), on the window of the chain the step reads: the
+    region, the previous region's vertex and enough sites on either side (an open
+    Heisenberg block) for the bonds to reach `cap`.  Building the state, its gauge and
+    the cached environments is not timed; the step itself is."""
+    import math
+    from oracle import sweep as osw
+    from oracle.network import G, ProjTTN, euler_sweep, from_network, orthogonalize
     import networksolvers_gb300.models as m
-    rng = np.random.default_rng(seed)
-    W = m.heisenberg_chain(4).tensors[2]  # bulk MPO tensor [left, s', s, right], w = 5
-    w, d = W.shape[0], W.shape[1]
-    a, b, s1, s2 = Index(chi), Index(chi), Index(d), Index(d)
-    w1, w2, w3 = Index(w), Index(w), Index(w)
-    L = rng.standard_normal((chi, w, chi)); L = L + L.transpose(2, 1, 0)
-    R = rng.standard_normal((chi, w, chi)); R = R + R.transpose(2, 1, 0)
-    Lt, Rt = Tensor(L, [a.prime(), w1, a]), Tensor(R, [b.prime(), w3, b])
-    W1, W2 = Tensor(W, [w1, s1.prime(), s1, w2]), Tensor(W, [w2, s2.prime(), s2, w3])
-    from oracle.tensor import contract
-    inds = [a, s1, s2, b]
-    hmap = lambda x: contract([Lt, W1, W2, Rt, Tensor(x, inds)], out=[i.prime() for i in inds]).data
-    times = []
-    for _ in range(nregions):
-        x0 = rng.standard_normal((chi, d, d, chi))
-        t = time.perf_counter()
-        lam, x = ok.eigsolve_lanczos(hmap, x0, krylovdim=3, maxiter=1)
-        U, Cc, err, sp = ol.factorize(Tensor(x, inds), [a, s1], cutoff=CUTOFF, maxdim=chi)
-        A = U
-        Lnew = contract([Lt, A, W1, A.dag().prime()], out=[U.inds[-1].prime(), w2, U.inds[-1]])
-        times.append(time.perf_counter() - t)
-    return float(np.mean(times)), nregions
+    cg = m.chain_graph(N_SITES)
+    plan = euler_sweep(G(cg.vertices, cg.edges), 2)
+    region = list(plan[position][0])
+    prev = list(plan[position - 1][0]) if position > 0 else list(plan[-1][0])
+    lb = int(math.ceil(math.log2(cap))) + 1
+    lo = max(1, min(region + prev) - lb)
+    hi = min(N_SITES, max(region + prev) + lb)
+    nw = hi - lo + 1
+    g = m.chain_graph(nw)
+    sub = lambda v: v - lo + 1
+    H = m.heisenberg_chain(nw)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    tensors, legs = {}, {}
+    for v in g.vertices:
+        lg = m._permuted_legs(g, v, 'l', [('s', v)])
+        shape = []
+        for leg in lg:
+            if leg[0] == 's':
+                shape.append(2)
+            else:
+                i = min(leg[1])  # bond between sub-chain sites i and i+1
+                ir = lo - 1 + i  # the same bond of the full chain
+                shape.append(int(min(cap, 2 ** min(i, nw - i, 30), 2 ** min(ir, N_SITES - ir, 30))))
+        tensors[v] = rng.standard_normal(shape)
+        legs[v] = lg
+    net = m.Network(g, tensors, legs, np.float64, {"kind": "state", "ortho_region": list(g.vertices)})
+    psi, sites = from_network(net)
+    (_, Ht), _ = from_network(H, site_index=sites)
+    a, b = sub(region[0]), sub(region[1])
+    pr = [sub(v) for v in prev]
+    psi = orthogonalize(psi, [a])
+    psi[a] = psi[a] / psi[a].norm()
+    P = ProjTTN(psi.g, Ht)
+    # environments the step reads from the cache: everything outside the region and the
+    # previous region's vertex
+    pv = [v for v in pr if v not in (a, b)]
+    for (u, v) in P.incident_edges(pr + [a, b]):
+        P.environment(psi, u, v)
+    P.position(psi, pr)
+    prob = osw.EigsolveProblem(psi, P)
+    kw = kwargs_for(0)
+    rkw = dict(extracter_kwargs=kw["extracter_kwargs"], updater_kwargs=kw["updater_kwargs"],
+               inserter_kwargs=kw["inserter_kwargs"], outputlevel=0)
+    R = osw.RegionIterator(prob, [(pr, rkw), ([a, b], rkw)])
+    R.which = 1
+    t = time.perf_counter()
+    osw.region_iterator_action(prob, R, osw.updater_eigsolve, sweep=sweep, **rkw)
+    return time.perf_counter() - t, (pv, len(pr))
+
+
+def cpu_sweep_sample(sweeps, caps, seed=11):
+    """One oracle region step per sweep in `sweeps` (largest bond `caps[k]`), at region
+    positions spread evenly over the sweep (stratified: step k runs region
+    floor((k + 1/2) 198 / len(sweeps))).  Returns the per-step seconds."""
+    out = []
+    n = len(sweeps)
+    for k, (sw, cap) in enumerate(zip(sweeps, caps)):
+        pos = int((k + 0.5) * REGIONS_PER_SWEEP / n)
+        t, _ = cpu_region_step(sw, pos, cap, seed + k)
+        out.append(t)
+    return out
 
 
 def run_reference(args):
-    """CPU reference arm: the oracle (FP64 numpy/OpenBLAS, all host threads)."""
+    """CPU reference arm: the oracle (FP64 numpy/OpenBLAS on all host threads) running
+    region steps of the workload's sweeps W+1..W+K, one region per step (W warm-up steps
+    before them); sweeps/s = regions run / 198 / their measured time."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    steps = []
-    for k in range(args.warmup + args.steps):
-        t_region, _ = cpu_region_sample(nregions=1, seed=100 + k)
-        if k >= args.warmup:
-            steps.append(t_region * REGIONS_PER_SWEEP)
-    t = float(np.mean(steps))
-    v = 1.0 / t
+    warm = list(range(1, args.warmup + 1))
+    timed = list(range(args.warmup + 1, args.warmup + args.steps + 1))
+    cpu_sweep_sample(warm, [sweep_bond(s) for s in warm], seed=5)
+    steps = cpu_sweep_sample(timed, [sweep_bond(s) for s in timed])
+    t = float(np.sum(steps))
+    v = args.steps / REGIONS_PER_SWEEP / t
     cores = os.cpu_count()
     line = {"impl": "reference", "metric": "dmrg_sweeps_per_s", "value": v, "unit": "sweeps/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3,
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3 / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "global_batch": 1,
-                       "seq_len": N_SITES, "parallelism": "none"},
+            "config": config_dict(1),
             "cpu_baseline": {"value": v, "unit": "sweeps/s", "cores": cores, "kind": "port",
-                             "sample": "one steady-state region step per step (bond dim 1024: Lanczos with 3 H_eff "
-                                       "applications, truncated SVD, environment update) x 198 regions per sweep"},
+                             "sample": f"one oracle region step per step (densitymatrix expansion, Lanczos with 3 "
+                                       f"H_eff applications, truncated factorization) of sweeps {timed[0]}-{timed[-1]}"
+                                       f" at region positions spread evenly over the sweep, bond dimensions "
+                                       f"{sorted(set(sweep_bond(s) for s in timed))} as the sweeps reach them; "
+                                       f"value = steps / 198 / measured time"},
+            "step_seconds": steps,
             "e2e": {"value": v, "unit": "sweeps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def config_dict(world):
+    return {"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "global_batch": world, "seq_len": N_SITES,
+            "parallelism": f"replicas{world}"}
 
 
 def run_nsg(args):
@@ -200,14 +275,23 @@ def run_nsg(args):
     from networksolvers_gb300.sweep import EigsolveProblem, sweep_solve, updater_eigsolve
     from networksolvers_gb300.network import euler_sweep
     prob = EigsolveProblem(psi, P)
-    energies, maxdims, sweep_ms = [], [], []
+    energies, maxdims, sweep_ms, all_ms = [], [], [], []
     plan = lambda: euler_sweep(psi.g, 2, **dict(extracter_kwargs=kw["extracter_kwargs"],
                                                  updater_kwargs=kw["updater_kwargs"],
                                                  inserter_kwargs=kw["inserter_kwargs"], outputlevel=0))
+    from networksolvers_gb300.sweep import RegionIterator, region_iterator_action
+
+    def one_sweep(sweep):
+        nonlocal prob
+        pl = plan()
+        R = RegionIterator(prob, pl)
+        for k, (region, rkws) in enumerate(pl):
+            R.which = k
+            prob = region_iterator_action(prob, R, updater_eigsolve, sweep=sweep, **dict(rkws))
+
     total = args.warmup + args.steps
     clocks = Clocks()
-    prof = None
-    launches0 = None
+    launches0 = launches1 = 0
     for sweep in range(1, total + 1):
         timed = sweep > args.warmup
         if timed and sweep == args.warmup + 1:
@@ -219,32 +303,33 @@ def run_nsg(args):
                 td.barrier()
             ctx.synchronize()
             clocks.start()
-            ctx.profile(True)
             launches0 = ctx.counters()["launches"]
         ctx.record(0)
-        # one sweep of the schedule (sweep index drives get_or_last)
-        from networksolvers_gb300.sweep import RegionIterator, region_iterator_action
-        pl = plan()
-        R = RegionIterator(prob, pl)
-        for k, (region, rkws) in enumerate(pl):
-            R.which = k
-            kws = dict(rkws)
-            prob = region_iterator_action(prob, R, updater_eigsolve, sweep=sweep, **kws)
+        one_sweep(sweep)  # one sweep of the schedule (the sweep index drives get_or_last)
         ctx.record(1)
         ms = ctx.elapsed_ms(0, 1)
+        all_ms.append(ms)
         energies.append(prob.eigenvalue)
         maxdims.append(prob.state.maxlinkdim())
         if timed:
             sweep_ms.append(ms)
     ctx.synchronize()
+    launches1 = ctx.counters()["launches"]
     if dist:
         td.barrier()
-    prof = ctx.profile_read()
-    ctx.profile(False)
-    launches = ctx.counters()["launches"] - launches0
     clk = clocks.stop()
+    launches = launches1 - launches0
     t_sweep = replica_time(float(np.sum(sweep_ms)) / 1e3, device="cuda" if dist else None)
     value = replica_throughput(world, args.steps, t_sweep)
+    # kernel shares and the roofline come from one further sweep with CUDA events around
+    # every launch of the profiled kernel classes (outside the timed sweeps)
+    ctx.profile(True)
+    ctx.record(0)
+    one_sweep(total + 1)
+    ctx.record(1)
+    prof_sweep_ms = ctx.elapsed_ms(0, 1)
+    prof = ctx.profile_read()
+    ctx.profile(False)
     # e2e: the timed sweeps again through the public API from host buffers, one `dmrg`
     # call per sweep (upload of the state and the operator, environments built from
     # scratch, the sweep, download of the state), from the host copy taken before them
@@ -265,7 +350,7 @@ def run_nsg(args):
         e2e = {"value": args.steps / (t1 - t0), "unit": "sweeps/s", "h2d_bytes_per_step": int(h2d // args.steps),
                "d2h_bytes_per_step": int(d2h // args.steps), "energy": E2}
     bf16, hbm, kind = peaks()
-    # roofline of the dominant kernel class in the timed region
+    # roofline of the dominant kernel class of the profiled sweep
     classes = {k: v for k, v in prof.items() if v["launches"] > 0}
     dom = max(classes, key=lambda k: classes[k]["ms"]) if classes else None
     tot_ms = sum(v["ms"] for v in classes.values())
@@ -284,10 +369,10 @@ def run_nsg(args):
     elif dom is not None:
         c = classes[dom]
         achieved = c["flops"] / (c["ms"] / 1e3) / 1e12
-        fp64_peak = 1.25
+        fp64_peak = FP64_PEAK_TFLOPS
         roof = {"bound": "fp64", "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp64_peak, "traffic": None, "kernel": dom,
-                "peak_note": "GB300 FP64 rate (no FP64 figure in the measured peaks; 1.25 TFLOP/s nominal)"}
+                "peak_note": FP64_PEAK_NOTE}
         if dom == "tridiag":
             # DRAM bytes of one launch from the ncu capture at n = 1024 (8.44 MB read + 1.83 MB
             # written: the L2-resident matrix once, the reflectors back), scaled by n^2 to the
@@ -296,28 +381,39 @@ def run_nsg(args):
             roof["traffic"] = 10.27e6 * (n_eff / 1024.0) ** 2
             roof["traffic_note"] = (f"bytes per launch at the launches' mean order n = {n_eff:.0f} (from 4/3 n^3 "
                                     f"flops per launch), scaled by n^2 from ncu at n=1024")
+    if roof is not None:
+        roof["measured_in"] = f"sweep {total + 1} (CUDA events around each launch of the class; outside the timed sweeps)"
     tc = classes.get("tc_gemm")
     heff_tflops = (tc["flops"] / (tc["ms"] / 1e3) / 1e12) if tc else None
     cpu = None
     if rank == 0 and not args.no_cpu:
-        t_region, nreg = cpu_region_sample(nregions=1)
-        cpu = {"value": 1.0 / (t_region * REGIONS_PER_SWEEP), "unit": "sweeps/s", "cores": os.cpu_count(),
-               "kind": "port", "sample": f"{nreg} steady-state region step(s) at bond dimension 1024 (Lanczos with "
-                                         f"3 H_eff applications, truncated SVD, environment update) x 198 regions"}
+        timed_sweeps = list(range(args.warmup + 1, total + 1))
+        secs = cpu_sweep_sample(timed_sweeps, maxdims[args.warmup:total])
+        cv = args.steps / REGIONS_PER_SWEEP / float(np.sum(secs))
+        cpu = {"value": cv, "unit": "sweeps/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"one oracle region step per timed sweep ({args.steps} steps, {float(np.sum(secs)):.1f} s), "
+                         f"region positions spread evenly over the sweep, at the largest bond dimension each timed "
+                         f"sweep reached; value = steps / 198 / measured time"}
+    tts = None
+    if total >= 10:
+        tts = {"sweeps": 10, "seconds": float(np.sum(all_ms[:10])) / 1e3, "energy": energies[9],
+               "note": "the configuration's 10-sweep run (sweeps 1-10 of this run, CUDA events); timed sweeps past "
+                       "sweep 10 repeat the converged state"}
     if rank == 0:
+        cfg = config_dict(world)
+        cfg.update({"timed_sweeps": list(range(args.warmup + 1, args.warmup + args.steps + 1)),
+                    "maxdim_schedule": SCHEDULE, "precision": args.precision,
+                    "l2": "operands 8-170 MB per GEMM at bond dim >= 512 (larger than L2)"})
         line = {"metric": "dmrg_sweeps_per_s", "value": value, "unit": "sweeps/s", "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_sweep * 1e3 / args.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64" if args.precision == "fp64" else f"{args.precision}+f64",
-                "data": "synthetic",
-                "config": {"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "global_batch": world,
-                           "seq_len": N_SITES, "parallelism": f"replicas{world}",
-                           "timed_sweeps": list(range(args.warmup + 1, args.warmup + args.steps + 1)),
-                           "maxdim_schedule": SCHEDULE, "precision": args.precision,
-                           "l2": "operands 8-170 MB per GEMM at bond dim >= 512 (larger than L2)"},
+                "data": "synthetic", "config": cfg,
                 "energy": energies[-1], "energies_per_sweep": energies, "maxlinkdim_per_sweep": maxdims,
-                "sweep_ms": sweep_ms, "heff_gemm_tflops_fp64_equiv": heff_tflops,
+                "sweep_ms": sweep_ms, "all_sweep_ms": all_ms, "time_to_solution": tts,
+                "heff_gemm_tflops_fp64_equiv": heff_tflops,
                 "kernel_share": {k: v["ms"] / tot_ms for k, v in classes.items()} if tot_ms else {},
+                "profiled_sweep_ms": prof_sweep_ms,
                 "roofline": roof, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": int(launches),
                 "launches_before_timed": int(launches0),
                 "clocks": clk}

@@ -101,6 +101,14 @@ int nsg_ctx_event_elapsed(nsg_ctx* ctx, int slot_from, int slot_to, float* ms);
 int nsg_ctx_profile(nsg_ctx* ctx, int enable);
 int nsg_ctx_profile_read(nsg_ctx* ctx, int cls, uint64_t* launches, double* ms, double* flops);
 
+/* Diagnostic of the timeout path (no counterpart in the reference): launches a kernel
+ * that waits on the context's stream, with the bounded pattern of the library's own
+ * device waits, for a device flag that nothing sets.  After `polls` polls (1..2^24, each
+ * about 0.1 us) the wait gives up, raises the context's error flag and the call returns
+ * NSG_ERR_TIMEOUT; the context stays usable.  Hosts use it to check that they turn
+ * that status into an error. */
+int nsg_ctx_wait_probe(nsg_ctx* ctx, int64_t polls);
+
 /* ---- tensors ------------------------------------------------------------- */
 int nsg_tensor_create(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims, nsg_tensor** out);
 int nsg_tensor_upload(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims,
@@ -223,10 +231,12 @@ int nsg_region_step(nsg_ctx* ctx, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2,
  * cudaFree or allocating library routine: the operand slices and the device error
  * flag live in one static device array of 64 MiB (plus a 256-byte header), held by
  * every GPU that loads the library until the process exits; sizes whose padded slices
- * exceed it are rejected with NSG_ERR_UNSUPPORTED.  The first call on a device
- * resolves that array's address and configures the kernel (with the device current);
- * make that first call before any stream capture.  All calls share the array: calls
- * that overlap on the GPU (other streams, other threads) race on it.  On failure the
+ * exceed it (or any extent above 2^23) are rejected with NSG_ERR_UNSUPPORTED.  The
+ * first call on a device resolves that array's address and configures the kernel (with
+ * the device current).  Every call synchronises `stream` and reads the error flag back
+ * into host memory, so the entry point cannot be called while `stream` is being
+ * captured into a CUDA graph.  All calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race on it.  On failure the
  * message is written to errbuf (errlen bytes, NUL-terminated). */
 int nsg_gemm_tf32x3_noalloc(const double* A, int64_t lda, int transA, const double* B, int64_t ldb,
                             int transB, double* C, int64_t ldc, int64_t M, int64_t N, int64_t K,

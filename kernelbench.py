@@ -1,9 +1,9 @@
 """Single-kernel timings of the sweep's hot operations on the library stream.
 
-    python -m networksolvers_gb300.kernelbench factorize --n 1024 [--complex] [--precision fp64]
-    python -m networksolvers_gb300.kernelbench heff --chi 512 [--precision ozaki]
-    python -m networksolvers_gb300.kernelbench gemm --m 4096 --n 4096 --k 4096 [--precision ozaki]
-    python -m networksolvers_gb300.kernelbench region --chi 1024 --chi-right 512 [--precision ozaki]
+    python kernelbench.py factorize --n 1024 [--complex] [--precision fp64]
+    python kernelbench.py heff --chi 512 [--precision ozaki]
+    python kernelbench.py gemm --m 4096 --n 4096 --k 4096 [--precision ozaki]
+    python kernelbench.py region --chi 1024 --chi-right 512 [--precision ozaki]
 
 `factorize` is the inserter's truncated factorization (it.factorize, inserter.jl:23) of
 an n x n two-site matrix keeping n/2 states; `heff` one application of the two-site
@@ -24,12 +24,15 @@ from __future__ import annotations
 import argparse
 import json
 import sys
+from pathlib import Path
 
 import numpy as np
 
-from . import _native
-from .itensors import DTensor, Index, contract, factorize
-from .network import LinearMap
+sys.path.insert(0, str(Path(__file__).resolve().parent))
+
+from networksolvers_gb300 import _native  # noqa: E402
+from networksolvers_gb300.itensors import DTensor, Index, contract, factorize  # noqa: E402
+from networksolvers_gb300.network import LinearMap  # noqa: E402
 
 
 class _FixedMap:
@@ -43,7 +46,7 @@ class _FixedMap:
 
 
 def _heff_case(chi, seed):
-    from .models import heisenberg_chain
+    from networksolvers_gb300.models import heisenberg_chain
     rng = np.random.default_rng(seed)
     W = heisenberg_chain(4).tensors[2]  # bulk MPO tensor [left, s', s, right]
     w, d = W.shape[0], W.shape[1]
@@ -61,9 +64,9 @@ def _heff_case(chi, seed):
 
 
 def _region_case(chi, chi_right, precision, seed, ctx):
-    from . import models
-    from .network import euler_sweep
-    from .sweep import EigsolveProblem, RegionIterator, _prepare, region_iterator_action, updater_eigsolve
+    from networksolvers_gb300 import models
+    from networksolvers_gb300.network import euler_sweep
+    from networksolvers_gb300.sweep import EigsolveProblem, RegionIterator, _prepare, region_iterator_action, updater_eigsolve
     nsites = 24
     g = models.chain_graph(nsites)
     mid = nsites // 2
@@ -97,7 +100,7 @@ def _region_case(chi, chi_right, precision, seed, ctx):
 
 
 def main(argv=None):
-    ap = argparse.ArgumentParser(prog="python -m networksolvers_gb300.kernelbench")
+    ap = argparse.ArgumentParser(prog="python kernelbench.py")
     ap.add_argument("op", choices=["factorize", "heff", "gemm", "region"])
     ap.add_argument("--n", type=int, default=1024)
     ap.add_argument("--m", type=int, default=4096)

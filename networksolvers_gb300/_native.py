@@ -51,6 +51,7 @@ _SIGS = {
     "nsg_ctx_event_elapsed": (i32, [p, i32, i32, C.POINTER(C.c_float)]),
     "nsg_ctx_profile": (i32, [p, i32]),
     "nsg_ctx_profile_read": (i32, [p, i32, C.POINTER(u64), P_dbl, P_dbl]),
+    "nsg_ctx_wait_probe": (i32, [p, i64]),
     "nsg_tensor_create": (i32, [p, i32, i32, P_i64, P_p]),
     "nsg_tensor_upload": (i32, [p, i32, i32, P_i64, p, P_p]),
     "nsg_tensor_download": (i32, [p, p, p]),

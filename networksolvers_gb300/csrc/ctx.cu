@@ -3,12 +3,34 @@
 
 #include <cstring>
 #include <cmath>
+#include <map>
+#include <mutex>
+#include <utility>
 
 namespace nsg {
 
 void check_launch(const char* what) {
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) throw Error(NSG_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+void bind_device(const nsg_ctx* c) {
+  if (!c) return;
+  int cur = -1;
+  NSG_CUDA(cudaGetDevice(&cur));
+  if (cur != c->device) NSG_CUDA(cudaSetDevice(c->device));
+}
+
+void ensure_smem_limit(const void* fn, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<int, const void*>, int> limit;
+  int dev = 0;
+  NSG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> g(mu);
+  int& cur = limit[{dev, fn}];
+  if (bytes <= cur) return;
+  NSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+  cur = bytes;
 }
 
 void* dalloc(nsg_ctx* c, size_t bytes) {
@@ -109,11 +131,36 @@ double* dev_scratch(nsg_ctx* c, size_t n) {
   return c->dev_scratch;
 }
 
+// Waits for a device flag with the bounded pattern of the library's kernels (poll,
+// back off, give up after `polls` polls) and, when the wait runs out, raises the
+// context's error flag and returns: the context stays usable.
+__global__ void wait_probe_kernel(const int* flag, long long polls, int* err) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const volatile int* f = flag;
+  for (long long i = 0; i < polls; ++i) {
+    if (*f) return;
+    __nanosleep(64);
+  }
+  atomicExch(err, 1);
+}
+
 }  // namespace nsg
 
 using namespace nsg;
 
 extern "C" {
+
+int nsg_ctx_wait_probe(nsg_ctx* c, int64_t polls) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c, NSG_ERR_INVALID, "null context");
+  NSG_CHECK(polls >= 1 && polls <= (int64_t(1) << 24), NSG_ERR_INVALID, "wait probe: polls must be in [1, 2^24]");
+  ScopedBuf flag(c, sizeof(int));  // zeroed, and nothing ever sets it
+  NSG_CUDA(cudaMemsetAsync(flag.p, 0, sizeof(int), c->stream));
+  wait_probe_kernel<<<1, 32, 0, c->stream>>>((const int*)flag.p, (long long)polls, device_flag(c));
+  count_launch(c);
+  check_launch("wait probe");
+  NSG_API_END(c)
+}
 
 int nsg_ctx_create(int device, uint64_t hbm_budget_bytes, nsg_ctx** out) {
   nsg_ctx* c = nullptr;

@@ -236,17 +236,7 @@ __global__ void __launch_bounds__(kSkinnyRows)
   }
 }
 
-// Raise a kernel's dynamic shared-memory limit once per process (set to the most any
-// call can ask for, so concurrent contexts never see a lower one).
-void raise_smem_limit_gemm(const void* fn, int bytes) {
-  static std::mutex mu;
-  static std::map<const void*, int> limit;
-  std::lock_guard<std::mutex> lk(mu);
-  int& cur = limit[fn];
-  if (bytes <= cur) return;
-  NSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  cur = bytes;
-}
+void raise_smem_limit_gemm(const void* fn, int bytes) { ensure_smem_limit(fn, bytes); }
 
 }  // namespace
 

@@ -476,7 +476,8 @@ bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
   const int64_t ab = (g.strideA == 0) ? 1 : g.batch, bb = (g.strideB == 0) ? 1 : g.batch;
   size_t nA = size_t(S) * Mp * Kp * ab, nB = size_t(S) * Np * Kp * bb;
   size_t bytes = 2 * (nA + nB) + 8 * (size_t(Mp) * ab + size_t(Np) * bb) + 256;
-  unsigned char* buf = (unsigned char*)dalloc(c, bytes);
+  ScopedBuf sbuf(c, bytes);
+  unsigned char* buf = (unsigned char*)sbuf.p;
   __nv_bfloat16* As = (__nv_bfloat16*)buf;
   __nv_bfloat16* Bs = As + nA;
   double* sa = (double*)(((uintptr_t)(Bs + nB) + 255) & ~(uintptr_t)255);
@@ -485,12 +486,7 @@ bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
   slice_operand<S>(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
   CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM, S), mB = make_map(Bs, Np, Kp, S * bb, BN, S);
   int* err = device_flag(c);  // checked once at the end of the public call
-  static std::once_flag attr;  // one per instantiation; contexts on other threads race here
-  cudaError_t attr_err = cudaSuccess;
-  std::call_once(attr, [&] {
-    attr_err = cudaFuncSetAttribute(oz_gemm_kernel<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-  });
-  NSG_CUDA(attr_err);
+  ensure_smem_limit((const void*)oz_gemm_kernel<S>, SMEM_BYTES);
   OzEpi ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, sa, sb, Mp, Np,
            ab > 1, bb > 1, err};
   dim3 grid(unsigned(Mp / BM), unsigned(Np / BN), unsigned(g.batch));
@@ -500,7 +496,6 @@ bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
   }
   count_launch(c);
   check_launch("oz_gemm");
-  dfree(c, buf, bytes);
   return true;
 }
 

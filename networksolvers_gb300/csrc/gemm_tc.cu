@@ -380,8 +380,8 @@ bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g) {
   const int64_t ab = (aB == 0) ? 1 : g.batch, bb = (bB == 0) ? 1 : g.batch;
   if (g.batch > 1 && (ab == 1 || bb == 1)) return false;
   size_t szA = size_t(Mp) * Kp * ab, szB = size_t(Np) * Kp * bb;
-  float* buf = (float*)dalloc(c, sizeof(float) * 2 * (szA + szB));
-  float* Ah = buf;
+  ScopedBuf sbuf(c, sizeof(float) * 2 * (szA + szB));
+  float* Ah = (float*)sbuf.p;
   float* Al = Ah + szA;
   float* Bh = Al + szA;
   float* Bl = Bh + szB;
@@ -389,20 +389,9 @@ bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g) {
   split_operand(c, (const double*)g.B, g.N, g.K, brs, bks, bB, bb, Np, Kp, Bh, Bl);
   CUtensorMap mAh = make_map(Ah, Mp, Kp, ab, TM), mAl = make_map(Al, Mp, Kp, ab, TM);
   CUtensorMap mBh = make_map(Bh, Np, Kp, bb, BN), mBl = make_map(Bl, Np, Kp, bb, BN);
-  int* err = (int*)dev_scratch(c, 1);  // first slot of the reduction scratch
-  NSG_CUDA(cudaMemsetAsync(err, 0, sizeof(int), c->stream));
-  static std::once_flag attr;  // contexts on other threads race here
-  cudaError_t attr_err = cudaSuccess;
-  std::call_once(attr, [&] {
-    attr_err = cudaFuncSetAttribute(tc_gemm_tf32x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-  });
-  NSG_CUDA(attr_err);
+  int* err = device_flag(c);  // checked once at the end of the public call
+  ensure_smem_limit((const void*)tc_gemm_tf32x3_kernel, SMEM_BYTES);
   EpiParams ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, err};
-  if (g.batch > 1 && (ab == 1 || bb == 1)) {
-    // a batch with one operand shared (the small operator tensors) stays on the FP64 path
-    dfree(c, buf, sizeof(float) * 2 * (szA + szB));
-    return false;
-  }
   dim3 grid(unsigned(Mp / TM), unsigned(Np / BN), unsigned(g.batch));
   {
   ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(g.M) * double(g.N) * double(g.K) * double(g.batch));
@@ -410,11 +399,6 @@ bool gemm_split_tc(nsg_ctx* c, const GemmArgs& g) {
   }
   count_launch(c);
   check_launch("tc_gemm_tf32x3");
-  dfree(c, buf, sizeof(float) * 2 * (szA + szB));
-  int herr = 0;
-  NSG_CUDA(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  NSG_CUDA(cudaStreamSynchronize(c->stream));
-  NSG_CHECK(herr == 0, NSG_ERR_TIMEOUT, "tc_gemm: a bounded mbarrier wait timed out");
   return true;
 }
 
@@ -469,6 +453,12 @@ extern "C" int nsg_gemm_tf32x3_noalloc(const double* A, int64_t lda, int transA,
     NSG_CHECK(A && B && C && M > 0 && N > 0 && K > 0, NSG_ERR_INVALID, "noalloc gemm: null operand or empty size");
     NSG_CHECK(lda >= (transA ? K : M) && ldb >= (transB ? N : K) && ldc >= M, NSG_ERR_INVALID,
               "noalloc gemm: leading dimension too small");
+    // each extent alone below the scratch's element count, so the padded sizes and their
+    // product below cannot wrap (at most 2 x 2^24 x 2^24 x 8 bytes)
+    constexpr int64_t kMaxExtent = int64_t(kNoAllocSliceBytes / 8);
+    NSG_CHECK(M <= kMaxExtent && N <= kMaxExtent && K <= kMaxExtent, NSG_ERR_UNSUPPORTED,
+              "noalloc gemm: an extent exceeds " + std::to_string(kMaxExtent) +
+                  ", beyond the static scratch maximum (use the allocating entry points)");
     const int64_t Mp = (M + TM - 1) / TM * TM, Np = (N + BN - 1) / BN * BN, Kp = (K + BK - 1) / BK * BK;
     const size_t need = sizeof(float) * 2 * size_t(Mp + Np) * size_t(Kp);
     NSG_CHECK(need <= kNoAllocSliceBytes, NSG_ERR_UNSUPPORTED,

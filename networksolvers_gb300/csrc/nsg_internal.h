@@ -80,6 +80,22 @@ inline size_t elem_bytes(int dtype) { return dtype == NSG_C128 ? 16 : 8; }
 // memory
 void* dalloc(nsg_ctx* c, size_t bytes);
 void dfree(nsg_ctx* c, void* p, size_t bytes);
+// Device buffer from the context's pool, returned to it when the scope ends (also when
+// a later step of the same call throws).
+struct ScopedBuf {
+  nsg_ctx* c;
+  void* p = nullptr;
+  size_t bytes = 0;
+  ScopedBuf(nsg_ctx* cc, size_t b) : c(cc), bytes(b) { p = dalloc(c, b); }
+  ~ScopedBuf() {
+    try {
+      dfree(c, p, bytes);
+    } catch (...) {
+    }
+  }
+  ScopedBuf(const ScopedBuf&) = delete;
+  ScopedBuf& operator=(const ScopedBuf&) = delete;
+};
 nsg_tensor* new_tensor(nsg_ctx* c, int dtype, int rank, const int64_t* dims, bool zero = false);
 void free_tensor(nsg_ctx* c, nsg_tensor* t);
 double* host_scalars(nsg_ctx* c, size_t n);
@@ -112,6 +128,14 @@ struct ProfScope {
   }
 };
 void check_launch(const char* what);
+// Make the context's device current on the calling thread (every public entry point
+// does this first, so a context created for device k works from any thread).
+void bind_device(const nsg_ctx* c);
+// Raise a kernel's dynamic shared-memory limit on the current device, never lower it.
+// cudaFuncSetAttribute applies to the device current when it is called, and contexts on
+// other host threads (or devices) launch the same kernels concurrently with other sizes,
+// so the limit is tracked per (device, kernel) and only ever raised.
+void ensure_smem_limit(const void* fn, int bytes);
 
 // ---------------------------------------------------------------------------
 // kernels (launchers)
@@ -166,7 +190,7 @@ void tridiag_eig(int n, const double* alpha, const double* beta, double* evals, 
 }  // namespace nsg
 
 // extern "C" guard helper
-#define NSG_API_BEGIN(ctx) try {
+#define NSG_API_BEGIN(ctx) try { ::nsg::bind_device(ctx);
 #define NSG_API_END(ctx)                                                   \
   ::nsg::check_device_flag(ctx);                                           \
   }                                                                        \

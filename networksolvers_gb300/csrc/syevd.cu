@@ -26,18 +26,7 @@
 namespace nsg {
 
 
-// Raise a kernel's dynamic shared-memory limit, never lower it.  The attribute is
-// process-wide and contexts on other host threads launch the same kernels concurrently
-// with other sizes: a limit lowered by one of them would fail another's launch.
-static void raise_smem_limit(const void* fn, int bytes) {
-  static std::mutex mu;
-  static std::map<const void*, int> limit;
-  std::lock_guard<std::mutex> g(mu);
-  int& cur = limit[fn];
-  if (bytes <= cur) return;
-  NSG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
-  cur = bytes;
-}
+static void raise_smem_limit(const void* fn, int bytes) { ensure_smem_limit(fn, bytes); }
 
 namespace {
 

@@ -423,7 +423,7 @@ def test_fused_region_step_matches_call_by_call(nsg_ctx):
     """nsg_region_step (product, Lanczos, truncated factorization in one call) against
     the same region step taken entry point by entry point."""
     import networksolvers_gb300.models as models
-    from networksolvers_gb300.kernelbench import _FixedMap
+    from kernelbench import _FixedMap
     from networksolvers_gb300.network import LinearMap
     from networksolvers_gb300.sweep import eigsolve_solver, region_step
     rng = np.random.default_rng(11)
