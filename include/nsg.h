@@ -97,7 +97,8 @@ int nsg_ctx_event_elapsed(nsg_ctx* ctx, int slot_from, int slot_to, float* ms);
 #define NSG_PROF_SPLIT 1       /* FP64 -> TF32 slice pass                          */
 #define NSG_PROF_SIMT_GEMM 2   /* FP64 CUDA-core GEMM                              */
 #define NSG_PROF_TRIDIAG 3     /* Householder tridiagonalisation                   */
-#define NSG_PROF_NCLASS 4
+#define NSG_PROF_DC 4          /* divide and conquer: leaves, merges, secular roots */
+#define NSG_PROF_NCLASS 5
 int nsg_ctx_profile(nsg_ctx* ctx, int enable);
 int nsg_ctx_profile_read(nsg_ctx* ctx, int cls, uint64_t* launches, double* ms, double* flops);
 

@@ -12,7 +12,9 @@ Heisenberg MPO (w = 5, d = 2); `gemm` one plain product; `region` one full two-s
 DMRG region step (extracter with density-matrix expansion, Lanczos updater, inserter;
 iterators.jl:81-100) in the middle of a 24-site Heisenberg chain whose bonds are --chi
 left of the region and --chi-right from it on (the shape of a left-to-right sweep that
-raises the bond dimension from chi-right to chi), maxdim --chi.  For `region` the
+raises the bond dimension from chi-right to chi), maxdim --maxdim (default --chi; with
+--chi 475 --chi-right 475 --maxdim 1024 the shape of the converged N=100 sweep, where
+the expansion doubles the bond before the truncation brings it back).  For `region` the
 --warmup calls step the regions before the timed ones, so every timed call is the next
 region of the same sweep.  Each runs --warmup untimed
 and --reps timed calls and prints one JSON line with the mean time per call (CUDA
@@ -63,7 +65,7 @@ def _heff_case(chi, seed):
     return LinearMap(_FixedMap(fixed), inds), x
 
 
-def _region_case(chi, chi_right, precision, seed, ctx):
+def _region_case(chi, chi_right, precision, seed, ctx, maxdim=None):
     from networksolvers_gb300 import models
     from networksolvers_gb300.network import euler_sweep
     from networksolvers_gb300.sweep import EigsolveProblem, RegionIterator, _prepare, region_iterator_action, updater_eigsolve
@@ -83,7 +85,7 @@ def _region_case(chi, chi_right, precision, seed, ctx):
     H = models.heisenberg_chain(nsites)
     psi, P = _prepare(H, psi0, ctx)
     prob = EigsolveProblem(psi, P)
-    trunc = dict(cutoff=1e-12, maxdim=chi)
+    trunc = dict(cutoff=1e-12, maxdim=maxdim or chi)
     plan = euler_sweep(psi.g, 2)
     R = RegionIterator(prob, plan)
     first = [k for k, (region, _) in enumerate(plan) if region[0] == mid][0]
@@ -107,6 +109,9 @@ def main(argv=None):
     ap.add_argument("--k", type=int, default=4096)
     ap.add_argument("--chi", type=int, default=512)
     ap.add_argument("--chi-right", type=int, default=None)
+    ap.add_argument("--maxdim", type=int, default=None,
+                    help="region: truncation maxdim (default --chi); above --chi the densitymatrix expansion "
+                         "enlarges the bond as in a converged sweep of a larger maxdim")
     ap.add_argument("--complex", action="store_true")
     ap.add_argument("--precision", default="fp64", choices=sorted(_native.PRECISIONS))
     ap.add_argument("--warmup", type=int, default=1)
@@ -134,8 +139,9 @@ def main(argv=None):
         flops = lm.flops()
         case = {"chi": args.chi, "w": 5, "d": 2}
     elif args.op == "region":
-        run = _region_case(args.chi, args.chi_right or args.chi // 2, args.precision, args.seed, ctx)
-        case = {"chi": args.chi, "chi_right": args.chi_right or args.chi // 2, "sites": 24}
+        run = _region_case(args.chi, args.chi_right or args.chi // 2, args.precision, args.seed, ctx, args.maxdim)
+        case = {"chi": args.chi, "chi_right": args.chi_right or args.chi // 2, "sites": 24,
+                "maxdim": args.maxdim or args.chi}
     else:
         i, j, l = Index(args.m), Index(args.n), Index(args.k)
         A = DTensor.from_numpy(rng.standard_normal((args.m, args.k)), [i, l])

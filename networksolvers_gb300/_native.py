@@ -155,7 +155,7 @@ class Context:
         self.check(self.L.nsg_ctx_profile(self.h, int(enable)))
 
     def profile_read(self):
-        names = ["tc_gemm", "split", "simt_gemm", "tridiag"]
+        names = ["tc_gemm", "split", "simt_gemm", "tridiag", "dc"]
         out = {}
         for k, nm in enumerate(names):
             n, ms, fl = u64(), dbl(), dbl()

@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <functional>
 #include <map>
 #include <mutex>
@@ -551,126 +552,50 @@ __global__ void __launch_bounds__(32 * kLeafWarps)
 }
 
 
-// Per merge (one CTA, serial parts on thread 0): gather D and z, flip for rho < 0,
-// sort, normalise z, deflate.  Outputs (per merge, arrays of length nb = hi - lo, at
-// offset lo in the workspace):
-//   Ds[a]   sorted (flipped) poles, perm[a] local column of sorted slot a
-//   zs[a]   normalised z (0 for deflated)
-//   kind[a] 1 = non-deflated, 0 = deflated
-//   rot     Givens list (local cols p, q, c, s) in application order
-// and scalars: rho (after normalisation), k, nrot, flip.
-struct MergeWork {
-  double* Ds;
-  double* zs;
-  int* perm;
-  int* kind;
-  int* rot_pq;     // 2 per rotation
-  double* rot_cs;  // 2 per rotation
-  double* rho;     // per merge
-  int* counts;     // per merge: k, nrot, flip
+// Merges of the divide and conquer, one tree level at a time: every kernel below
+// handles all merges of a level in one launch (blockIdx.y or the warp index selects the
+// merge), so a level costs a fixed handful of launches and one host read of the
+// deflation counts, whatever the number of merges.
+//
+// Workspace (device arrays of length n; a merge uses the slice [lo, hi) of each):
+//   Ds, zs     sorted (sign-flipped) poles and normalised z, 0 for deflated slots
+//   perm       block-local column of sorted slot t
+//   kind       1 = non-deflated, 0 = deflated
+//   kinv       sorted slot of the q-th non-deflated pole
+//   Dk, zk     the non-deflated poles and weights, compacted
+//   lam, zh    secular roots and Gu-Eisenstat weights (first k entries)
+//   srck, srci, wn   final ordering: source kind / index and eigenvalue of output column
+//   rot_pq, rot_cs   deflation rotations (2 entries each per rotation, at 2 lo)
+//   gscr       scratch of the serial steps for blocks above the shared-memory limit
+// Per merge: rho, counts (k, nrot, flip).
+struct DcWork {
+  double *Ds, *zs, *Dk, *zk, *lam, *zh, *wn, *rot_cs, *gscr;
+  int *perm, *kind, *kinv, *srck, *srci, *rot_pq;
+  double* rho;
+  int* counts;
 };
 
-__global__ void merge_prep_kernel(const double* w, const double* Q, int n, const MergeDesc* md, int nmerge,
-                                  MergeWork W) {
-  int mi = blockIdx.x;
-  if (mi >= nmerge || threadIdx.x != 0) return;
-  const MergeDesc M = md[mi];
-  const int lo = M.lo, mid = M.mid, hi = M.hi, nb = hi - lo, n1 = mid - lo;
-  double rho = M.beta;
-  int flip = rho < 0;
-  double sg = flip ? -1.0 : 1.0;
-  if (flip) rho = -rho;
-  double* Ds = W.Ds + lo;
-  double* zs = W.zs + lo;
-  int* perm = W.perm + lo;
-  int* kind = W.kind + lo;
-  // merge the two ascending halves after the sign flip (descending halves when flipped)
-  int a = 0, b = 0;
-  for (int t = 0; t < nb; ++t) {
-    int ia = flip ? (n1 - 1 - a) : a;         // local index into half 1
-    int ib = flip ? (nb - 1 - b) : (n1 + b);  // local index into half 2
-    bool takeA;
-    if (a >= n1)
-      takeA = false;
-    else if (b >= nb - n1)
-      takeA = true;
-    else
-      takeA = sg * w[lo + ia] <= sg * w[lo + ib];
-    int li = takeA ? ia : ib;
-    if (takeA)
-      ++a;
-    else
-      ++b;
-    perm[t] = li;
-    Ds[t] = sg * w[lo + li];
-    // z: last row of block 1 / first row of block 2 (Q block rows in global coordinates)
-    zs[t] = (li < n1) ? Q[(size_t)(lo + li) * n + (mid - 1)] : Q[(size_t)(lo + li) * n + mid];
-  }
-  double nz = 0.0;
-  for (int t = 0; t < nb; ++t) nz += zs[t] * zs[t];
-  nz = sqrt(nz);
-  rho = rho * nz * nz;
-  double dmax = 0.0;
-  for (int t = 0; t < nb; ++t) {
-    zs[t] /= nz;
-    dmax = fmax(dmax, fabs(Ds[t]));
-  }
-  const double tol = 8.0 * 2.220446049250313e-16 * fmax(dmax, rho);
-  int k = 0, nrot = 0, prev = -1;
-  int* rpq = W.rot_pq + 2 * lo;
-  double* rcs = W.rot_cs + 2 * lo;
-  for (int t = 0; t < nb; ++t) {
-    if (rho * fabs(zs[t]) <= tol) {
-      kind[t] = 0;
-      zs[t] = 0.0;
-      continue;
-    }
-    kind[t] = 1;
-    if (prev >= 0 && fabs(Ds[t] - Ds[prev]) <= tol) {
-      double r = hypot(zs[t], zs[prev]);
-      double c = zs[t] / r, s = zs[prev] / r;
-      double dp = Ds[prev], dt = Ds[t];
-      Ds[prev] = c * c * dp + s * s * dt;
-      Ds[t] = s * s * dp + c * c * dt;
-      zs[prev] = 0.0;
-      zs[t] = r;
-      kind[prev] = 0;
-      rpq[2 * nrot] = perm[prev];
-      rpq[2 * nrot + 1] = perm[t];
-      rcs[2 * nrot] = c;
-      rcs[2 * nrot + 1] = s;
-      ++nrot;
-    }
-    prev = t;
-  }
-  for (int t = 0; t < nb; ++t) k += kind[t];
-  W.rho[mi] = rho;
-  W.counts[3 * mi] = k;
-  W.counts[3 * mi + 1] = nrot;
-  W.counts[3 * mi + 2] = flip;
-}
+constexpr int kSmemMerge = 4096;  // rows of a block whose serial steps run in shared memory
 
-// Shared-memory forms of the three serial steps of a merge (preparation with
-// deflation, compaction of the non-deflated slots, final ordering).  The CTA loads the
-// merge's data in parallel; the order-dependent loops then run in one thread on shared
-// memory (a few cycles per element instead of a global round trip), and the results are
-// written back in parallel.  Used for blocks of up to kSmemMerge rows.
-constexpr int kSmemMerge = 4096;  // 48 bytes of shared memory per row at most
-
-__global__ void merge_prep_smem_kernel(const double* w, const double* Q, int n, const MergeDesc* md, int nmerge,
-                                       MergeWork W) {
-  extern __shared__ double mp_smem[];
+// Per merge (one CTA): gather the two halves' eigenvalues and the z vector (last row of
+// block 1, first row of block 2), flip for rho < 0, merge the ascending halves, normalise
+// z, deflate (small z_t; poles closer than tol rotated together), apply the deflation
+// rotations to the block's columns of Q, and compact the non-deflated poles.
+__global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict__ Q, int n,
+                               const MergeDesc* __restrict__ md, DcWork W) {
+  extern __shared__ double dp_smem[];
   const int mi = blockIdx.x;
-  if (mi >= nmerge) return;
   const MergeDesc M = md[mi];
   const int lo = M.lo, mid = M.mid, hi = M.hi, nb = hi - lo, n1 = mid - lo;
-  double* ws = mp_smem;       // block eigenvalues
-  double* zr = ws + nb;       // z candidates by local index
-  double* Dsm = zr + nb;      // sorted D
-  double* zsm = Dsm + nb;     // sorted z
-  int* pm = (int*)(zsm + nb);  // sorted -> local index
-  int* kd = pm + nb;           // kind
-  __shared__ double red[32];
+  const bool sm = nb <= kSmemMerge;
+  double* ws = sm ? dp_smem : W.gscr + 2 * (size_t)lo;  // block eigenvalues by local index
+  double* zr = ws + nb;                                  // z candidates by local index
+  double* Dsm = sm ? zr + nb : W.Ds + lo;
+  double* zsm = sm ? Dsm + nb : W.zs + lo;
+  int* pm = sm ? (int*)(zsm + nb) : W.perm + lo;
+  int* kd = sm ? pm + nb : W.kind + lo;
+  __shared__ double red[32], redm[32];
+  __shared__ int s_nrot;
   for (int li = threadIdx.x; li < nb; li += blockDim.x) {
     ws[li] = w[lo + li];
     zr[li] = (li < n1) ? Q[(size_t)(lo + li) * n + (mid - 1)] : Q[(size_t)(lo + li) * n + mid];
@@ -714,7 +639,6 @@ __global__ void merge_prep_smem_kernel(const double* w, const double* Q, int n, 
     dm = fmax(dm, __shfl_xor_sync(0xffffffffu, dm, o));
   }
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  __shared__ double redm[32];
   if (lane == 0) {
     red[warp] = s2;
     redm[warp] = dm;
@@ -729,11 +653,11 @@ __global__ void merge_prep_smem_kernel(const double* w, const double* Q, int n, 
   rho = rho * nz * nz;
   for (int t = threadIdx.x; t < nb; t += blockDim.x) zsm[t] /= nz;
   __syncthreads();
+  int* rpq = W.rot_pq + 2 * lo;
+  double* rcs = W.rot_cs + 2 * lo;
   if (threadIdx.x == 0) {
     const double tol = 8.0 * 2.220446049250313e-16 * fmax(dmax, rho);
     int k = 0, nrot = 0, prev = -1;
-    int* rpq = W.rot_pq + 2 * lo;
-    double* rcs = W.rot_cs + 2 * lo;
     for (int t = 0; t < nb; ++t) {
       if (rho * fabs(zsm[t]) <= tol) {
         kd[t] = 0;
@@ -758,69 +682,248 @@ __global__ void merge_prep_smem_kernel(const double* w, const double* Q, int n, 
       }
       prev = t;
     }
-    for (int t = 0; t < nb; ++t) k += kd[t];
+    // compaction of the non-deflated slots
+    int* kinv = W.kinv + lo;
+    double* Dk = W.Dk + lo;
+    double* zk = W.zk + lo;
+    for (int t = 0; t < nb; ++t) {
+      if (kd[t]) {
+        kinv[k] = t;
+        Dk[k] = Dsm[t];
+        zk[k] = zsm[t];
+        ++k;
+      }
+    }
     W.rho[mi] = rho;
     W.counts[3 * mi] = k;
     W.counts[3 * mi + 1] = nrot;
     W.counts[3 * mi + 2] = flip;
+    s_nrot = nrot;
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
-    W.Ds[lo + t] = Dsm[t];
-    W.zs[lo + t] = zsm[t];
-    W.perm[lo + t] = pm[t];
-    W.kind[lo + t] = kd[t];
-  }
-}
-
-__global__ void gather_nondeflated_smem_kernel(int nb, const int* kind, const double* Ds, const double* zs, int* kpos,
-                                               double* Dk, double* zk) {
-  extern __shared__ int gn_smem[];
-  int* kd = gn_smem;
-  int* kp = kd + nb;
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) kd[t] = kind[t];
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int k = 0;
-    for (int t = 0; t < nb; ++t) {
-      kp[t] = kd[t] ? k : -1;
-      k += kd[t];
+  if (sm) {
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      W.Ds[lo + t] = Dsm[t];
+      W.zs[lo + t] = zsm[t];
+      W.perm[lo + t] = pm[t];
+      W.kind[lo + t] = kd[t];
     }
   }
-  __syncthreads();
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
-    const int q = kp[t];
-    kpos[t] = q;
-    if (q >= 0) {
-      Dk[q] = Ds[t];
-      zk[q] = zs[t];
+  // the deflation rotations, in order, on the block's columns of Q (one row per thread)
+  const int nrot = s_nrot;
+  if (nrot > 0) {
+    for (int r = threadIdx.x; r < nb; r += blockDim.x) {
+      double* row = Q + (lo + r);
+      for (int q = 0; q < nrot; ++q) {
+        const size_t cp = (size_t)(lo + rpq[2 * q]) * n, ci = (size_t)(lo + rpq[2 * q + 1]) * n;
+        const double c = rcs[2 * q], sn = rcs[2 * q + 1];
+        const double xp = row[cp], xi = row[ci];
+        row[cp] = c * xp - sn * xi;
+        row[ci] = sn * xp + c * xi;
+      }
     }
   }
 }
 
-__global__ void merge_finalize_order_smem_kernel(const double* Ds, const int* kind, const double* lam, int nb, int flip,
-                                                 int* src_kind, int* src_idx, double* wout) {
-  extern __shared__ double mf_smem[];
-  double* Dsm = mf_smem;
-  double* lm = Dsm + nb;
-  double* wo = lm + nb;
-  int* kd = (int*)(wo + nb);
-  int* sk = kd + nb;
-  int* si = sk + nb;
-  __shared__ int s_nr;
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
-    Dsm[t] = Ds[t];
-    kd[t] = kind[t];
+// Secular roots: one warp per (merge, root).  Root i of 1 + rho sum_j z_j^2 / (D_j - lambda)
+// lies in (D_i, D_{i+1}) (the last one in (D_{k-1}, D_{k-1} + rho)); it is represented as
+// origin + tau with the origin at the nearer pole, so D_j - lambda = (D_j - origin) - tau
+// is exact enough for the Gu-Eisenstat vectors.  Iteration: the two-pole rational model
+// of Bunch, Nielsen and Sorensen (psi for poles j <= i, phi for j > i, each matched in
+// value and slope at tau), solved as a quadratic inside the bracket; bisection when the
+// model step leaves the bracket.  Delta_m[i * k + j] = D_j - lambda_i (block of kmax^2).
+__global__ void dc_secular_kernel(const MergeDesc* __restrict__ md, int nm, int kmax, DcWork W,
+                                  double* __restrict__ Delta_all) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (gw >= (int64_t)nm * kmax) return;
+  const int mi = int(gw / kmax), i = int(gw % kmax);
+  const int k = W.counts[3 * mi];
+  if (i >= k) return;
+  const int lo = md[mi].lo;
+  const double* Dk = W.Dk + lo;
+  const double* zk = W.zk + lo;
+  const double rho = W.rho[mi];
+  double* Delta = Delta_all + (size_t)mi * kmax * kmax;
+  const double eps = 2.220446049250313e-16;
+  int org;
+  double blo, bhi;
+  if (i < k - 1) {
+    const double gap = Dk[i + 1] - Dk[i];
+    const double mid = 0.5 * gap;  // relative to D_i
+    double f = 0.0;
+    for (int j = lane; j < k; j += 32) f += rho * zk[j] * zk[j] / ((Dk[j] - Dk[i]) - mid);
+    for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
+    f += 1.0;
+    if (f >= 0) {
+      org = i;
+      blo = 0.0;
+      bhi = mid;
+    } else {
+      org = i + 1;
+      blo = -mid;
+      bhi = 0.0;
+    }
+  } else {
+    org = k - 1;
+    blo = 0.0;
+    bhi = rho;
   }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    int nr = 0;
-    for (int t = 0; t < nb; ++t) nr += kd[t];
-    s_nr = nr;
+  const double dorg = Dk[org];
+  const double ddi = Dk[i] - dorg;
+  const double ddi1 = (i < k - 1) ? Dk[i + 1] - dorg : 0.0;
+  double tau = 0.5 * (blo + bhi);
+  for (int it = 0; it < 100; ++it) {
+    double psi = 0.0, dpsi = 0.0, phi = 0.0, dphi = 0.0, fa = 0.0;
+    for (int j = lane; j < k; j += 32) {
+      const double del = (Dk[j] - dorg) - tau;
+      const double q = zk[j] / del;
+      const double term = rho * zk[j] * q;
+      const double dterm = rho * q * q;
+      if (j <= i) {
+        psi += term;
+        dpsi += dterm;
+      } else {
+        phi += term;
+        dphi += dterm;
+      }
+      fa += fabs(term);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      psi += __shfl_xor_sync(0xffffffffu, psi, o);
+      dpsi += __shfl_xor_sync(0xffffffffu, dpsi, o);
+      phi += __shfl_xor_sync(0xffffffffu, phi, o);
+      dphi += __shfl_xor_sync(0xffffffffu, dphi, o);
+      fa += __shfl_xor_sync(0xffffffffu, fa, o);
+    }
+    const double f = 1.0 + psi + phi;
+    if (f > 0)
+      bhi = tau;
+    else
+      blo = tau;
+    if (fabs(f) <= 4.0 * eps * (k + 1.0) * (1.0 + fa)) break;
+    if (bhi - blo <= 2.0 * eps * fmax(fabs(blo), fabs(bhi)) || bhi - blo < 1e-300) break;
+    double tn;
+    const double di = ddi - tau;
+    const double b1 = dpsi * di * di, a1 = psi - b1 / di;
+    if (i < k - 1) {
+      const double di1 = ddi1 - tau;
+      const double b2 = dphi * di1 * di1, a2 = phi - b2 / di1;
+      const double C = 1.0 + a1 + a2;
+      // C (ddi - x)(ddi1 - x) + b1 (ddi1 - x) + b2 (ddi - x) = 0
+      const double qa = C, qb = -(C * (ddi + ddi1) + b1 + b2), qc = C * ddi * ddi1 + b1 * ddi1 + b2 * ddi;
+      tn = NAN;
+      if (qa != 0.0) {
+        const double disc = qb * qb - 4.0 * qa * qc;
+        if (disc >= 0.0) {
+          const double sq = sqrt(disc);
+          const double qq = -0.5 * (qb + copysign(sq, qb));
+          const double r1 = qq / qa, r2 = (qq != 0.0) ? qc / qq : NAN;
+          if (r1 > blo && r1 < bhi)
+            tn = r1;
+          else if (r2 > blo && r2 < bhi)
+            tn = r2;
+        }
+      } else if (qb != 0.0) {
+        tn = -qc / qb;
+      }
+    } else {
+      // 1 + phi_const + a1 + b1/(ddi - x) = 0 with phi == 0
+      const double C = 1.0 + a1 + phi;
+      tn = (C != 0.0) ? ddi + b1 / C : NAN;
+    }
+    if (!(tn > blo && tn < bhi)) tn = 0.5 * (blo + bhi);
+    if (tn == tau) break;
+    tau = tn;
   }
-  __syncthreads();
-  const int nr = s_nr, nd = nb - nr;
-  for (int t = threadIdx.x; t < nr; t += blockDim.x) lm[t] = lam[t];
+  if (lane == 0) W.lam[lo + i] = dorg + tau;
+  for (int j = lane; j < k; j += 32) Delta[(size_t)i * k + j] = (Dk[j] - dorg) - tau;
+}
+
+// Gu-Eisenstat: zhat_j^2 = (lam_j - D_j)/rho * prod_{i != j} (lam_i - D_j)/(D_i - D_j);
+// one warp per (merge, j).
+__global__ void dc_gu_eisenstat_kernel(const MergeDesc* __restrict__ md, int nm, int kmax, DcWork W,
+                                       const double* __restrict__ Delta_all) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (gw >= (int64_t)nm * kmax) return;
+  const int mi = int(gw / kmax), j = int(gw % kmax);
+  const int k = W.counts[3 * mi];
+  if (j >= k) return;
+  const int lo = md[mi].lo;
+  const double* Dk = W.Dk + lo;
+  const double* Delta = Delta_all + (size_t)mi * kmax * kmax;
+  double p = 1.0;
+  for (int i = lane; i < k; i += 32)
+    if (i != j) p *= (-Delta[(size_t)i * k + j]) / (Dk[i] - Dk[j]);
+  for (int o = 16; o > 0; o >>= 1) p *= __shfl_xor_sync(0xffffffffu, p, o);
+  p *= -Delta[(size_t)j * k + j] / W.rho[mi];
+  if (lane == 0) W.zh[lo + j] = copysign(sqrt(fmax(p, 0.0)), W.zk[lo + j]);
+}
+
+// S^T of each merge (kmax x kmax, column-major, zero outside its k x k block: column i =
+// normalised eigenvector of root i); one warp per (merge, column).
+__global__ void dc_vectors_kernel(const MergeDesc* __restrict__ md, int nm, int kmax, DcWork W,
+                                  const double* __restrict__ Delta_all, double* __restrict__ St_all) {
+  const int lane = threadIdx.x & 31;
+  const int64_t gw = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+  if (gw >= (int64_t)nm * kmax) return;
+  const int mi = int(gw / kmax), i = int(gw % kmax);
+  const int k = W.counts[3 * mi];
+  double* St = St_all + (size_t)mi * kmax * kmax + (size_t)i * kmax;
+  if (i >= k) {
+    for (int j = lane; j < kmax; j += 32) St[j] = 0.0;
+    return;
+  }
+  const double* zh = W.zh + md[mi].lo;
+  const double* Delta = Delta_all + (size_t)mi * kmax * kmax + (size_t)i * k;
+  double nrm = 0.0;
+  for (int j = lane; j < k; j += 32) {
+    const double s = zh[j] / Delta[j];
+    nrm += s * s;
+  }
+  for (int o = 16; o > 0; o >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
+  nrm = 1.0 / sqrt(nrm);
+  for (int j = lane; j < kmax; j += 32) St[j] = (j < k) ? zh[j] / Delta[j] * nrm : 0.0;
+}
+
+// The non-deflated (rotated) columns of each block, compacted into an nbmax x kmax
+// matrix per merge (zero padded); blockIdx.y = merge.
+__global__ void dc_gather_kernel(const double* __restrict__ Q, int n, const MergeDesc* __restrict__ md, int nbmax,
+                                 int kmax, DcWork W, double* __restrict__ Qk_all) {
+  const int mi = blockIdx.y;
+  const int lo = md[mi].lo, nb = md[mi].hi - lo, k = W.counts[3 * mi];
+  double* Qk = Qk_all + (size_t)mi * nbmax * kmax;
+  const size_t tot = (size_t)nbmax * kmax;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
+    const int r = int(e % nbmax), q = int(e / nbmax);
+    double v = 0.0;
+    if (r < nb && q < k) v = Q[(size_t)(lo + W.perm[lo + W.kinv[lo + q]]) * n + (lo + r)];
+    Qk[e] = v;
+  }
+}
+
+// Final ordering of each block (one CTA per merge): eigenvalues = roots (non-deflated)
+// and deflated poles, signs undone, ascending; the source of each output column.
+__global__ void dc_order_kernel(const MergeDesc* __restrict__ md, DcWork W) {
+  extern __shared__ double mo_smem[];
+  const int mi = blockIdx.x;
+  const int lo = md[mi].lo, nb = md[mi].hi - lo;
+  const int nr = W.counts[3 * mi], flip = W.counts[3 * mi + 2], nd = nb - nr;
+  const bool sm = nb <= kSmemMerge;
+  double* Dsm = sm ? mo_smem : W.Ds + lo;
+  double* lm = sm ? Dsm + nb : W.lam + lo;
+  double* wo = sm ? lm + nb : W.wn + lo;
+  int* kd = sm ? (int*)(wo + nb) : W.kind + lo;
+  int* sk = sm ? kd + nb : W.srck + lo;
+  int* si = sm ? sk + nb : W.srci + lo;
+  if (sm) {
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      Dsm[t] = W.Ds[lo + t];
+      kd[t] = W.kind[lo + t];
+    }
+    for (int t = threadIdx.x; t < nr; t += blockDim.x) lm[t] = W.lam[lo + t];
+  }
   __syncthreads();
   if (threadIdx.x == 0) {
     int ia = 0, ib = 0, pos = 0, dslot = 0;
@@ -851,262 +954,46 @@ __global__ void merge_finalize_order_smem_kernel(const double* Ds, const int* ki
     }
   }
   __syncthreads();
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
-    src_kind[t] = sk[t];
-    src_idx[t] = si[t];
-    wout[t] = wo[t];
-  }
-}
-
-// Apply the deflation rotations to the block's columns: one thread per row.
-__global__ void merge_rot_kernel(double* Q, int n, const MergeDesc* md, int mi, MergeWork W, int nrot) {
-  const MergeDesc M = md[mi];
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  int nb = M.hi - M.lo;
-  if (r >= nb) return;
-  const int* rpq = W.rot_pq + 2 * M.lo;
-  const double* rcs = W.rot_cs + 2 * M.lo;
-  double* row = Q + (M.lo + r);
-  for (int q = 0; q < nrot; ++q) {
-    size_t cp = (size_t)(M.lo + rpq[2 * q]) * n, ci = (size_t)(M.lo + rpq[2 * q + 1]) * n;
-    double c = rcs[2 * q], s = rcs[2 * q + 1];
-    double xp = row[cp], xi = row[ci];
-    row[cp] = c * xp - s * xi;
-    row[ci] = s * xp + c * xi;
-  }
-}
-
-// Secular roots: one warp per root.  Root i of 1 + rho sum_j z_j^2 / (D_j - lambda) lies
-// in (D_i, D_{i+1}) (the last one in (D_{k-1}, D_{k-1} + rho)); it is represented as
-// origin + tau with the origin at the nearer pole, so D_j - lambda = (D_j - origin) - tau
-// is exact enough for the Gu-Eisenstat vectors.  Iteration: the two-pole rational model
-// of Bunch, Nielsen and Sorensen (psi for poles j <= i, phi for j > i, each matched in
-// value and slope at tau), solved as a quadratic inside the bracket; bisection when the
-// model step leaves the bracket.  Delta[i * k + j] = D_j - lambda_i.
-__global__ void secular_kernel(const double* Dk, const double* zk, int k, double rho, double* lam,
-                               double* Delta) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= k) return;
-  const double eps = 2.220446049250313e-16;
-  int org;
-  double lo, hi;
-  if (i < k - 1) {
-    double gap = Dk[i + 1] - Dk[i];
-    double mid = 0.5 * gap;  // relative to D_i
-    double f = 0.0;
-    for (int j = lane; j < k; j += 32) f += rho * zk[j] * zk[j] / ((Dk[j] - Dk[i]) - mid);
-    for (int o = 16; o > 0; o >>= 1) f += __shfl_xor_sync(0xffffffffu, f, o);
-    f += 1.0;
-    if (f >= 0) {
-      org = i;
-      lo = 0.0;
-      hi = mid;
-    } else {
-      org = i + 1;
-      lo = -mid;
-      hi = 0.0;
-    }
-  } else {
-    org = k - 1;
-    lo = 0.0;
-    hi = rho;
-  }
-  const double dorg = Dk[org];
-  const double ddi = Dk[i] - dorg;
-  const double ddi1 = (i < k - 1) ? Dk[i + 1] - dorg : 0.0;
-  double tau = 0.5 * (lo + hi);
-  for (int it = 0; it < 100; ++it) {
-    double psi = 0.0, dpsi = 0.0, phi = 0.0, dphi = 0.0, fa = 0.0;
-    for (int j = lane; j < k; j += 32) {
-      double del = (Dk[j] - dorg) - tau;
-      double q = zk[j] / del;
-      double term = rho * zk[j] * q;
-      double dterm = rho * q * q;
-      if (j <= i) {
-        psi += term;
-        dpsi += dterm;
-      } else {
-        phi += term;
-        dphi += dterm;
-      }
-      fa += fabs(term);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      psi += __shfl_xor_sync(0xffffffffu, psi, o);
-      dpsi += __shfl_xor_sync(0xffffffffu, dpsi, o);
-      phi += __shfl_xor_sync(0xffffffffu, phi, o);
-      dphi += __shfl_xor_sync(0xffffffffu, dphi, o);
-      fa += __shfl_xor_sync(0xffffffffu, fa, o);
-    }
-    double f = 1.0 + psi + phi;
-    if (f > 0)
-      hi = tau;
-    else
-      lo = tau;
-    if (fabs(f) <= 4.0 * eps * (k + 1.0) * (1.0 + fa)) break;
-    if (hi - lo <= 2.0 * eps * fmax(fabs(lo), fabs(hi)) || hi - lo < 1e-300) break;
-    // rational model step
-    double tn;
-    double di = ddi - tau;  // distance to the left pole (< 0 ... > 0 by side)
-    double b1 = dpsi * di * di, a1 = psi - b1 / di;
-    if (i < k - 1) {
-      double di1 = ddi1 - tau;
-      double b2 = dphi * di1 * di1, a2 = phi - b2 / di1;
-      double C = 1.0 + a1 + a2;
-      // C (ddi - x)(ddi1 - x) + b1 (ddi1 - x) + b2 (ddi - x) = 0
-      double qa = C, qb = -(C * (ddi + ddi1) + b1 + b2), qc = C * ddi * ddi1 + b1 * ddi1 + b2 * ddi;
-      tn = NAN;
-      if (qa != 0.0) {
-        double disc = qb * qb - 4.0 * qa * qc;
-        if (disc >= 0.0) {
-          double sq = sqrt(disc);
-          double qq = -0.5 * (qb + copysign(sq, qb));
-          double r1 = qq / qa, r2 = (qq != 0.0) ? qc / qq : NAN;
-          if (r1 > lo && r1 < hi)
-            tn = r1;
-          else if (r2 > lo && r2 < hi)
-            tn = r2;
-        }
-      } else if (qb != 0.0) {
-        tn = -qc / qb;
-      }
-    } else {
-      // 1 + phi_const + a1 + b1/(ddi - x) = 0 with phi == 0
-      double C = 1.0 + a1 + phi;
-      tn = (C != 0.0) ? ddi + b1 / C : NAN;
-    }
-    if (!(tn > lo && tn < hi)) tn = 0.5 * (lo + hi);
-    if (tn == tau) break;
-    tau = tn;
-  }
-  if (lane == 0) lam[i] = dorg + tau;
-  for (int j = lane; j < k; j += 32) Delta[(size_t)i * k + j] = (Dk[j] - dorg) - tau;
-}
-
-// Gu-Eisenstat: zhat_j^2 = (lam_j - D_j)/rho * prod_{i != j} (lam_i - D_j)/(D_i - D_j);
-// one warp per j, the product accumulated in logarithm-free pairs per lane.
-__global__ void gu_eisenstat_kernel(const double* Dk, const double* zk, int k, double rho, const double* Delta,
-                                    double* zh) {
-  const int lane = threadIdx.x & 31;
-  const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (j >= k) return;
-  double p = 1.0;
-  for (int i = lane; i < k; i += 32)
-    if (i != j) p *= (-Delta[(size_t)i * k + j]) / (Dk[i] - Dk[j]);
-  for (int o = 16; o > 0; o >>= 1) p *= __shfl_xor_sync(0xffffffffu, p, o);
-  p *= -Delta[(size_t)j * k + j] / rho;
-  if (lane == 0) zh[j] = copysign(sqrt(fmax(p, 0.0)), zk[j]);
-}
-
-// S^T (k x k, column-major: column i = normalised eigenvector of root i); warp per i
-__global__ void secular_vectors_kernel(const double* zh, int k, const double* Delta, double* St) {
-  const int lane = threadIdx.x & 31;
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  if (i >= k) return;
-  double nrm = 0.0;
-  for (int j = lane; j < k; j += 32) {
-    double s = zh[j] / Delta[(size_t)i * k + j];
-    nrm += s * s;
-  }
-  for (int o = 16; o > 0; o >>= 1) nrm += __shfl_xor_sync(0xffffffffu, nrm, o);
-  nrm = 1.0 / sqrt(nrm);
-  for (int j = lane; j < k; j += 32) St[j + (size_t)i * k] = zh[j] / Delta[(size_t)i * k + j] * nrm;
-}
-
-// Gather the non-deflated (rotated) columns of the block into a contiguous nb x k matrix
-// and their poles / weights into Dk, zk.
-__global__ void gather_nondeflated_kernel(const double* Q, int n, int lo, int nb, const int* perm, const int* kind,
-                                          const double* Ds, const double* zs, int* kpos, double* Qk, double* Dk,
-                                          double* zk) {
-  // kpos: position of each sorted slot among the non-deflated ones (thread 0)
-  if (threadIdx.x == 0 && blockIdx.x == 0) {
-    int k = 0;
-    for (int t = 0; t < nb; ++t) {
-      kpos[t] = kind[t] ? k : -1;
-      if (kind[t]) {
-        Dk[k] = Ds[t];
-        zk[k] = zs[t];
-        ++k;
-      }
+  if (sm) {
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      W.srck[lo + t] = sk[t];
+      W.srci[lo + t] = si[t];
+      W.wn[lo + t] = wo[t];
     }
   }
 }
 
-__global__ void gather_cols_kernel(const double* Q, int n, int lo, int nb, const int* perm, const int* kpos, double* Qk) {
-  size_t tot = (size_t)nb * nb;
+// The merged block of every merge into T (same position as in Q): output column `out`
+// is merged column srci (src kind 1) or the deflated column of Q it came from; the new
+// eigenvalues into w.  blockIdx.y = merge.
+__global__ void dc_scatter_kernel(const double* __restrict__ Q, int n, const MergeDesc* __restrict__ md, int nbmax,
+                                  int kmax, DcWork W, const double* __restrict__ Qm_all, double* __restrict__ T,
+                                  double* __restrict__ w) {
+  const int mi = blockIdx.y;
+  const int lo = md[mi].lo, nb = md[mi].hi - lo;
+  const double* Qm = Qm_all + (size_t)mi * nbmax * kmax;
+  const size_t tot = (size_t)nb * nb;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    int r = int(e % nb), t = int(e / nb);
-    int kp = kpos[t];
-    if (kp < 0) continue;
-    Qk[r + (size_t)kp * nb] = Q[(size_t)(lo + perm[t]) * n + (lo + r)];
+    const int r = int(e % nb), out = int(e / nb);
+    const int src = W.srci[lo + out];
+    const double v = W.srck[lo + out] ? Qm[r + (size_t)src * nbmax]
+                                      : Q[(size_t)(lo + W.perm[lo + src]) * n + (lo + r)];
+    T[(size_t)(lo + out) * n + (lo + r)] = v;
   }
+  if (blockIdx.x == 0)
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) w[lo + t] = W.wn[lo + t];
 }
 
-// Final ordering of the block: eigenvalues = roots (non-deflated) and deflated poles,
-// signs undone, sorted ascending; writes the new block of Q (into Qnew, nb x nb) and w.
-__global__ void merge_finalize_order_kernel(const double* Ds, const int* kind, const double* lam, int nb, int flip,
-                                            int* src_kind, int* src_idx, double* wout) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  // roots (ascending in the flipped space) and deflated poles (ascending) merged
-  int nr = 0, nd = 0;
-  for (int t = 0; t < nb; ++t) {
-    if (kind[t])
-      ++nr;
-    else
-      ++nd;
-  }
-  int ia = 0, ib = 0, pos = 0;
-  int dslot = 0;
-  while (dslot < nb && kind[dslot]) ++dslot;
-  while (ia < nr || ib < nd) {
-    bool takeRoot;
-    if (ia >= nr)
-      takeRoot = false;
-    else if (ib >= nd)
-      takeRoot = true;
-    else
-      takeRoot = lam[ia] <= Ds[dslot];
-    int out = flip ? (nb - 1 - pos) : pos;
-    if (takeRoot) {
-      src_kind[out] = 1;
-      src_idx[out] = ia;
-      wout[out] = flip ? -lam[ia] : lam[ia];
-      ++ia;
-    } else {
-      src_kind[out] = 0;
-      src_idx[out] = dslot;
-      wout[out] = flip ? -Ds[dslot] : Ds[dslot];
-      ++ib;
-      ++dslot;
-      while (dslot < nb && kind[dslot]) ++dslot;
-    }
-    ++pos;
-  }
-}
-
-__global__ void merge_scatter_kernel(const double* Qold, int n, int lo, int nb, const int* perm, const double* Qmerged,
-                                     const int* src_kind, const int* src_idx, double* Qnew) {
-  size_t tot = (size_t)nb * nb;
+// T's merged blocks back into Q; blockIdx.y = merge.
+__global__ void dc_copy_kernel(const double* __restrict__ T, int n, const MergeDesc* __restrict__ md,
+                               double* __restrict__ Q) {
+  const int mi = blockIdx.y;
+  const int lo = md[mi].lo, nb = md[mi].hi - lo;
+  const size_t tot = (size_t)nb * nb;
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    int r = int(e % nb), out = int(e / nb);
-    double v;
-    if (src_kind[out])
-      v = Qmerged[r + (size_t)src_idx[out] * nb];
-    else
-      v = Qold[(size_t)(lo + perm[src_idx[out]]) * n + (lo + r)];
-    Qnew[r + (size_t)out * nb] = v;
+    const size_t idx = (size_t)(lo + e / nb) * n + (lo + e % nb);
+    Q[idx] = T[idx];
   }
-}
-
-__global__ void copy_block_kernel(const double* src, int nb, double* Q, int n, int lo, const double* wsrc, double* w) {
-  size_t tot = (size_t)nb * nb;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < tot; e += (size_t)gridDim.x * blockDim.x) {
-    int r = int(e % nb), cidx = int(e / nb);
-    Q[(size_t)(lo + cidx) * n + (lo + r)] = src[e];
-  }
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < (size_t)nb; e += (size_t)gridDim.x * blockDim.x)
-    w[lo + e] = wsrc[e];
 }
 
 // complex phases: T's subdiagonal is real by construction except possibly the last one
@@ -1208,16 +1095,28 @@ static void build_tree(int lo, int hi, std::vector<std::vector<MergeDesc>>& leve
   levels[depth].push_back(MergeDesc{lo, mid, hi, 0.0});
 }
 
+// Leaf order of the divide and conquer: the implicit-QL leaves are one warp each and
+// latency bound (a chain of FP64 square roots and divides per rotation), so small leaves
+// and more (batched) merge levels are cheaper.  NSG_DC_LEAF (4..32) overrides it.
+static int dc_leaf_size(int n) {
+  static int env = [] {
+    const char* s = std::getenv("NSG_DC_LEAF");
+    int v = s ? std::atoi(s) : 0;
+    return (v >= 4 && v <= kLeaf) ? v : 0;
+  }();
+  if (env) return env;
+  (void)n;
+  return 8;
+}
+
 // Eigen-decomposition of the real symmetric tridiagonal (d, e); Q: n x n (device,
-// column-major), w: eigenvalues ascending (device).
+// column-major), w: eigenvalues ascending (device).  Cuppen's divide and conquer with
+// every merge of a tree level batched into one launch per step.
 static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const std::vector<double>& e_in, double* Q,
                        double* w) {
   std::vector<std::vector<MergeDesc>> levels;
   std::vector<int> llo, lhi;
-  // leaves of 16 up to order 256 (the QL leaves are latency bound: FP64 chains), of 32
-  // above (each extra merge level costs a batch of launches); measured on GB300
-  const int leaf = n <= 256 ? 16 : kLeaf;
-  build_tree(0, n, levels, llo, lhi, 0, leaf);
+  build_tree(0, n, levels, llo, lhi, 0, dc_leaf_size(n));
   // modified diagonal: for each split subtract beta at the two touching diagonals
   std::vector<double> d = d_in;
   for (auto& lv : levels)
@@ -1238,119 +1137,131 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
   NSG_CUDA(cudaMemcpyAsync(dhi.p, lhi.data(), sizeof(int) * nleaf, cudaMemcpyHostToDevice, c->stream));
   DevBuf lerr(c, sizeof(int));
   NSG_CUDA(cudaMemsetAsync(lerr.p, 0, sizeof(int), c->stream));
-  leaf_ql_kernel<<<(nleaf + kLeafWarps - 1) / kLeafWarps, 32 * kLeafWarps, 0, c->stream>>>(
-      dd.as<double>(), de.as<double>(), dlo.as<int>(), dhi.as<int>(), nleaf, Q, n, w, lerr.as<int>());
+  {
+    ProfScope ps(c, NSG_PROF_DC, 0.0);
+    leaf_ql_kernel<<<(nleaf + kLeafWarps - 1) / kLeafWarps, 32 * kLeafWarps, 0, c->stream>>>(
+        dd.as<double>(), de.as<double>(), dlo.as<int>(), dhi.as<int>(), nleaf, Q, n, w, lerr.as<int>());
+  }
   count_launch(c);
   check_launch("dc leaves");
-  int leaf_failed = 0;
-  NSG_CUDA(cudaMemcpyAsync(&leaf_failed, lerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
-  NSG_CUDA(cudaStreamSynchronize(c->stream));
-  NSG_CHECK(leaf_failed == 0, NSG_ERR_NONFINITE, "eigensolver: a tridiagonal leaf did not converge");
-  // merges, deepest level first
-  MergeWork W;
-  DevBuf bDs(c, sizeof(double) * n), bzs(c, sizeof(double) * n), bperm(c, sizeof(int) * n), bkind(c, sizeof(int) * n),
-      brpq(c, sizeof(int) * 2 * n), brcs(c, sizeof(double) * 2 * n);
+  if (levels.empty()) {
+    int leaf_failed = 0;
+    NSG_CUDA(cudaMemcpyAsync(&leaf_failed, lerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaStreamSynchronize(c->stream));
+    NSG_CHECK(leaf_failed == 0, NSG_ERR_NONFINITE, "eigensolver: a tridiagonal leaf did not converge");
+    return;
+  }
+  // all levels' merge descriptors in one upload
+  std::vector<MergeDesc> all;
+  std::vector<size_t> off(levels.size());
+  for (int L = int(levels.size()) - 1; L >= 0; --L) {
+    off[L] = all.size();
+    all.insert(all.end(), levels[L].begin(), levels[L].end());
+  }
+  DevBuf bmd(c, sizeof(MergeDesc) * all.size());
+  NSG_CUDA(cudaMemcpyAsync(bmd.p, all.data(), sizeof(MergeDesc) * all.size(), cudaMemcpyHostToDevice, c->stream));
+  size_t maxm = 0;
+  for (auto& lv : levels) maxm = std::max(maxm, lv.size());
+  DevBuf bDs(c, sizeof(double) * n), bzs(c, sizeof(double) * n), bDk(c, sizeof(double) * n),
+      bzk(c, sizeof(double) * n), blam(c, sizeof(double) * n), bzh(c, sizeof(double) * n), bwn(c, sizeof(double) * n),
+      brcs(c, sizeof(double) * 2 * n), bscr(c, sizeof(double) * 2 * n), bperm(c, sizeof(int) * n),
+      bkind(c, sizeof(int) * n), bkinv(c, sizeof(int) * n), bsrck(c, sizeof(int) * n), bsrci(c, sizeof(int) * n),
+      brpq(c, sizeof(int) * 2 * n), brho(c, sizeof(double) * maxm), bcnt(c, sizeof(int) * 3 * maxm),
+      Tbuf(c, sizeof(double) * (size_t)n * n);
+  DcWork W;
   W.Ds = bDs.as<double>();
   W.zs = bzs.as<double>();
+  W.Dk = bDk.as<double>();
+  W.zk = bzk.as<double>();
+  W.lam = blam.as<double>();
+  W.zh = bzh.as<double>();
+  W.wn = bwn.as<double>();
+  W.rot_cs = brcs.as<double>();
+  W.gscr = bscr.as<double>();
   W.perm = bperm.as<int>();
   W.kind = bkind.as<int>();
+  W.kinv = bkinv.as<int>();
+  W.srck = bsrck.as<int>();
+  W.srci = bsrci.as<int>();
   W.rot_pq = brpq.as<int>();
-  W.rot_cs = brcs.as<double>();
+  W.rho = brho.as<double>();
+  W.counts = bcnt.as<int>();
+  std::vector<int> cnt(3 * maxm);
+  bool leaves_checked = false;
   for (int L = int(levels.size()) - 1; L >= 0; --L) {
-    auto& lv = levels[L];
-    int nm = int(lv.size());
-    DevBuf bmd(c, sizeof(MergeDesc) * nm), brho(c, sizeof(double) * nm), bcnt(c, sizeof(int) * 3 * nm);
-    W.rho = brho.as<double>();
-    W.counts = bcnt.as<int>();
-    NSG_CUDA(cudaMemcpyAsync(bmd.p, lv.data(), sizeof(MergeDesc) * nm, cudaMemcpyHostToDevice, c->stream));
-    int maxnb = 0;
-    for (auto& m : lv) maxnb = std::max(maxnb, m.hi - m.lo);
-    if (maxnb <= kSmemMerge) {
-      const int shm = maxnb * (6 * 8);
-      raise_smem_limit((const void*)merge_prep_smem_kernel, shm);
-      merge_prep_smem_kernel<<<nm, 256, shm, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
-    } else {
-      merge_prep_kernel<<<nm, 32, 0, c->stream>>>(w, Q, n, bmd.as<MergeDesc>(), nm, W);
+    const auto& lv = levels[L];
+    const int nm = int(lv.size());
+    const MergeDesc* md = bmd.as<MergeDesc>() + off[L];
+    int nbmax = 0;
+    for (auto& m : lv) nbmax = std::max(nbmax, m.hi - m.lo);
+    {
+      const int shm = nbmax <= kSmemMerge ? nbmax * 40 : 0;
+      if (shm) raise_smem_limit((const void*)dc_prep_kernel, shm);
+      ProfScope ps(c, NSG_PROF_DC, 0.0);
+      dc_prep_kernel<<<nm, 256, shm, c->stream>>>(w, Q, n, md, W);
     }
     count_launch(c);
     check_launch("dc prep");
-    std::vector<double> rho(nm);
-    std::vector<int> cnt(3 * nm);
-    NSG_CUDA(cudaMemcpyAsync(rho.data(), brho.p, sizeof(double) * nm, cudaMemcpyDeviceToHost, c->stream));
-    NSG_CUDA(cudaMemcpyAsync(cnt.data(), bcnt.p, sizeof(int) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(cnt.data(), W.counts, sizeof(int) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
+    int leaf_failed = 0;
+    if (!leaves_checked)
+      NSG_CUDA(cudaMemcpyAsync(&leaf_failed, lerr.p, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     NSG_CUDA(cudaStreamSynchronize(c->stream));
-    for (int mi = 0; mi < nm; ++mi) {
-      const MergeDesc& M = lv[mi];
-      int nb = M.hi - M.lo, k = cnt[3 * mi], nrot = cnt[3 * mi + 1], flip = cnt[3 * mi + 2];
-      if (nrot > 0) {
-        merge_rot_kernel<<<(nb + 127) / 128, 128, 0, c->stream>>>(Q, n, bmd.as<MergeDesc>(), mi, W, nrot);
-        count_launch(c);
-      }
-      DevBuf Dk(c, sizeof(double) * std::max(k, 1)), zk(c, sizeof(double) * std::max(k, 1)),
-          kpos(c, sizeof(int) * nb), lam(c, sizeof(double) * std::max(k, 1));
-      DevBuf Qk(c, sizeof(double) * (size_t)nb * std::max(k, 1)), Qm(c, sizeof(double) * (size_t)nb * std::max(k, 1));
-      if (nb <= kSmemMerge) {
-        const int shm = nb * 8;
-        raise_smem_limit((const void*)gather_nondeflated_smem_kernel, shm);
-        gather_nondeflated_smem_kernel<<<1, 256, shm, c->stream>>>(nb, W.kind + M.lo, W.Ds + M.lo, W.zs + M.lo,
-                                                                   kpos.as<int>(), Dk.as<double>(), zk.as<double>());
-      } else {
-        gather_nondeflated_kernel<<<1, 32, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, W.kind + M.lo,
-                                                           W.Ds + M.lo, W.zs + M.lo, kpos.as<int>(), Qk.as<double>(),
-                                                           Dk.as<double>(), zk.as<double>());
-      }
-      check_launch("dc gather");  // kpos indexes the next kernels: fail before they run
-      int gblocks = int(std::min<size_t>(((size_t)nb * nb + 255) / 256, (size_t)c->num_sms * 8));
-      gather_cols_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, kpos.as<int>(),
-                                                         Qk.as<double>());
-      count_launch(c, 2);
-      if (k > 0) {
-        DevBuf Delta(c, sizeof(double) * (size_t)k * k), zh(c, sizeof(double) * k),
-            St(c, sizeof(double) * (size_t)k * k);
-        int tb = 256, gb = (k * 32 + tb - 1) / tb;  // one warp per root
-        secular_kernel<<<gb, tb, 0, c->stream>>>(Dk.as<double>(), zk.as<double>(), k, rho[mi], lam.as<double>(),
-                                                 Delta.as<double>());
-        gu_eisenstat_kernel<<<gb, tb, 0, c->stream>>>(Dk.as<double>(), zk.as<double>(), k, rho[mi],
-                                                      Delta.as<double>(), zh.as<double>());
-        secular_vectors_kernel<<<gb, tb, 0, c->stream>>>(zh.as<double>(), k, Delta.as<double>(), St.as<double>());
-        count_launch(c, 3);
-        check_launch("dc secular");
-        GemmArgs g;
-        g.dtype = NSG_F64;
-        g.M = nb;
-        g.N = k;
-        g.K = k;
-        g.A = Qk.p;
-        g.lda = nb;
-        g.opA = OP_N;
-        g.B = St.p;
-        g.ldb = k;
-        g.opB = OP_N;
-        g.C = Qm.p;
-        g.ldc = nb;
-        g.batch = 1;
-        g.strideA = g.strideB = g.strideC = 0;
-        gemm_accurate(c, g);
-      }
-      DevBuf skind(c, sizeof(int) * nb), sidx(c, sizeof(int) * nb), wnew(c, sizeof(double) * nb),
-          Qnew(c, sizeof(double) * (size_t)nb * nb);
-      if (nb <= kSmemMerge) {
-        const int shm = nb * (3 * 8 + 3 * 4);
-        raise_smem_limit((const void*)merge_finalize_order_smem_kernel, shm);
-        merge_finalize_order_smem_kernel<<<1, 256, shm, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(),
-                                                                     nb, flip, skind.as<int>(), sidx.as<int>(),
-                                                                     wnew.as<double>());
-      } else {
-        merge_finalize_order_kernel<<<1, 32, 0, c->stream>>>(W.Ds + M.lo, W.kind + M.lo, lam.as<double>(), nb, flip,
-                                                             skind.as<int>(), sidx.as<int>(), wnew.as<double>());
-      }
-      check_launch("dc order");  // src_kind / src_idx index the scatter
-      merge_scatter_kernel<<<gblocks, 256, 0, c->stream>>>(Q, n, M.lo, nb, W.perm + M.lo, Qm.as<double>(),
-                                                           skind.as<int>(), sidx.as<int>(), Qnew.as<double>());
-      copy_block_kernel<<<gblocks, 256, 0, c->stream>>>(Qnew.as<double>(), nb, Q, n, M.lo, wnew.as<double>(), w);
-      count_launch(c, 3);
-      check_launch("dc merge");
+    if (!leaves_checked) {
+      NSG_CHECK(leaf_failed == 0, NSG_ERR_NONFINITE, "eigensolver: a tridiagonal leaf did not converge");
+      leaves_checked = true;
     }
+    int kmax = 0;
+    for (int mi = 0; mi < nm; ++mi) kmax = std::max(kmax, cnt[3 * mi]);
+    const int gxe = int(std::max<int64_t>(1, std::min<int64_t>(((int64_t)nbmax * nbmax + 255) / 256,
+                                                                 std::max<int64_t>(1, (int64_t)c->num_sms * 8 / nm))));
+    DevBuf Qm(c, sizeof(double) * (size_t)nm * nbmax * std::max(kmax, 1));
+    if (kmax > 0) {
+      DevBuf Delta(c, sizeof(double) * (size_t)nm * kmax * kmax), St(c, sizeof(double) * (size_t)nm * kmax * kmax),
+          Qk(c, sizeof(double) * (size_t)nm * nbmax * kmax);
+      const int64_t warps = (int64_t)nm * kmax;
+      const int tb = 256, gb = int((warps * 32 + tb - 1) / tb);
+      {
+        ProfScope ps(c, NSG_PROF_DC, 0.0);
+        dc_secular_kernel<<<gb, tb, 0, c->stream>>>(md, nm, kmax, W, Delta.as<double>());
+        dc_gu_eisenstat_kernel<<<gb, tb, 0, c->stream>>>(md, nm, kmax, W, Delta.as<double>());
+        dc_vectors_kernel<<<gb, tb, 0, c->stream>>>(md, nm, kmax, W, Delta.as<double>(), St.as<double>());
+        const int gxk = int(std::max<int64_t>(
+            1, std::min<int64_t>(((int64_t)nbmax * kmax + 255) / 256, std::max<int64_t>(1, (int64_t)c->num_sms * 8 / nm))));
+        dc_gather_kernel<<<dim3(gxk, nm), 256, 0, c->stream>>>(Q, n, md, nbmax, kmax, W, Qk.as<double>());
+      }
+      count_launch(c, 4);
+      check_launch("dc secular");
+      GemmArgs g;
+      g.dtype = NSG_F64;
+      g.M = nbmax;
+      g.N = kmax;
+      g.K = kmax;
+      g.A = Qk.p;
+      g.lda = nbmax;
+      g.opA = OP_N;
+      g.strideA = (int64_t)nbmax * kmax;
+      g.B = St.p;
+      g.ldb = kmax;
+      g.opB = OP_N;
+      g.strideB = (int64_t)kmax * kmax;
+      g.C = Qm.p;
+      g.ldc = nbmax;
+      g.strideC = (int64_t)nbmax * kmax;
+      g.batch = nm;
+      gemm_accurate(c, g);
+    }
+    {
+      const int shm = nbmax <= kSmemMerge ? nbmax * 36 : 0;
+      if (shm) raise_smem_limit((const void*)dc_order_kernel, shm);
+      ProfScope ps(c, NSG_PROF_DC, 0.0);
+      dc_order_kernel<<<nm, 256, shm, c->stream>>>(md, W);
+      dc_scatter_kernel<<<dim3(gxe, nm), 256, 0, c->stream>>>(Q, n, md, nbmax, std::max(kmax, 1), W, Qm.as<double>(),
+                                                             Tbuf.as<double>(), w);
+      dc_copy_kernel<<<dim3(gxe, nm), 256, 0, c->stream>>>(Tbuf.as<double>(), n, md, Q);
+    }
+    count_launch(c, 3);
+    check_launch("dc merge");
   }
 }
 
