@@ -542,19 +542,33 @@ def run_tdvp(args):
 
 
 def run_c3_accuracy(args):
-    """The large DMRG configuration run to its full 10 sweeps in the plain and in the split
-    form from the same initial state: the energies of both after every sweep, |dE/E| of
-    the final energies, and the per-sweep times (CUDA events) of each form."""
+    """The large DMRG configuration run to its full --sweeps (10) sweeps in several forms from
+    the same initial state (--forms, default "fp64,ozaki"; "fp64p" is the plain form from
+    the initial state perturbed by 1e-13 relative noise, a measure of how far rounding-level
+    differences carry through the truncations).  Per form: the energy after every sweep and
+    every region, the truncated bond dimension of every region, per-sweep times (CUDA
+    events) and the time to solution; against the plain form: |dE/E| per sweep and the
+    first region whose bond dimension differs."""
     import networksolvers_gb300 as ns
     from networksolvers_gb300 import _native
+    from networksolvers_gb300.models import Network
     ctx = _native.Context(0, precision="fp64")
     _native.set_default_context(ctx)
     H, psi0 = workload()
     kw = kwargs_for(0)
+    forms = [f for f in args.forms.split(",") if f]
+    if "fp64" not in forms:
+        forms = ["fp64"] + forms
     res = {}
-    for prec in ("fp64", args.precision):
+    for form in forms:
+        prec = "fp64" if form == "fp64p" else form
+        start = psi0
+        if form == "fp64p":
+            rng = np.random.Generator(np.random.PCG64(12345))
+            start = Network(psi0.graph, {v: t * (1.0 + 1e-13 * rng.standard_normal(t.shape))
+                                         for v, t in psi0.tensors.items()}, psi0.legs, np.float64, dict(psi0.meta))
         ctx.set_precision(prec)
-        ens, ms = [], []
+        ens, ms, regs = [], [], []
         ctx.synchronize()
         ctx.record(0)
 
@@ -564,16 +578,41 @@ def run_c3_accuracy(args):
             ctx.record(0)
             ens.append(prob.eigenvalue)
 
-        E, psi = ns.dmrg(H, psi0, nsweeps=args.sweeps, sweep_callback=cb, **kw)
-        res[prec] = (ens, ms, psi.maxlinkdim())
-    ep, es = res["fp64"][0], res[args.precision][0]
-    _line(metric="dmrg_energy_agreement", value=abs(es[-1] - ep[-1]) / abs(ep[-1]), unit="|dE/E|",
-          higher_is_better=False, steps=args.sweeps, warmup=0, ms_per_step=float(np.mean(res[args.precision][1])),
-          dtype=f"{args.precision}+f64 vs f64",
+        def rcb(prob, sweep, region, which, **k):
+            regs.append((sweep, which, prob.eigenvalue, prob.last_insert.get("newdim", -1),
+                         prob.last_insert.get("truncerr", 0.0)))
+
+        E, psi = ns.dmrg(H, start, nsweeps=args.sweeps, sweep_callback=cb, region_callback=rcb, **kw)
+        res[form] = dict(energies=ens, sweep_ms=ms, regions=np.array(regs), maxlinkdim=psi.maxlinkdim())
+    ref = res["fp64"]
+    out = {}
+    for form, r in res.items():
+        d = dict(energy=r["energies"][-1], time_to_solution_s=float(np.sum(r["sweep_ms"])) / 1e3,
+                 sweep_ms=r["sweep_ms"], energies=r["energies"], maxlinkdim=r["maxlinkdim"])
+        if form != "fp64":
+            d["rel_dE_per_sweep"] = [abs(a - b) / abs(b) for a, b in zip(r["energies"], ref["energies"])]
+            diff = np.nonzero(r["regions"][:, 3] != ref["regions"][:, 3])[0]
+            d["first_bond_difference"] = (None if len(diff) == 0 else
+                                          {"index": int(diff[0]), "sweep": int(r["regions"][diff[0], 0]),
+                                           "region": int(r["regions"][diff[0], 1]),
+                                           "newdim": int(r["regions"][diff[0], 3]),
+                                           "newdim_fp64": int(ref["regions"][diff[0], 3]),
+                                           "truncerr": float(r["regions"][diff[0], 4]),
+                                           "truncerr_fp64": float(ref["regions"][diff[0], 4])})
+            d["regions_with_bond_difference"] = int(len(diff))
+            rel = np.abs(r["regions"][:, 2] - ref["regions"][:, 2]) / np.abs(ref["regions"][:, 2])
+            d["max_region_rel_dE_before_first_bond_difference"] = float(np.max(rel[:diff[0]])) if len(diff) else \
+                float(np.max(rel))
+            d["speedup_vs_fp64"] = float(np.sum(ref["sweep_ms"])) / float(np.sum(r["sweep_ms"]))
+        out[form] = d
+    main_form = [f for f in forms if f not in ("fp64", "fp64p")]
+    mf = main_form[0] if main_form else "fp64"
+    _line(metric="dmrg_energy_agreement", value=out[mf].get("rel_dE_per_sweep", [0.0])[-1], unit="|dE/E|",
+          higher_is_better=False, steps=args.sweeps, warmup=0,
+          ms_per_step=float(np.mean(res[mf]["sweep_ms"])), dtype=f"{mf}+f64 vs f64",
           config={"workload": "heisenberg_chain_N100_2site_dmrg_maxdim1024", "sweeps": args.sweeps,
-                  "maxdim_schedule": SCHEDULE, "cutoff": CUTOFF},
-          energies={"fp64": ep, args.precision: es}, sweep_ms={"fp64": res["fp64"][1], args.precision: res[args.precision][1]},
-          maxlinkdim={"fp64": res["fp64"][2], args.precision: res[args.precision][2]})
+                  "maxdim_schedule": SCHEDULE, "cutoff": CUTOFF, "forms": forms},
+          forms=out)
 
 
 def _pool_jobs_c4(count):
@@ -754,6 +793,8 @@ def main():
     ap.add_argument("--duration", type=float, default=30.0)
     ap.add_argument("--seed", type=int, default=0)
     ap.add_argument("--sweeps", type=int, default=10)
+    ap.add_argument("--forms", default="fp64,ozaki", help="accuracy workload: forms to run (fp64, ozaki, "
+                                                          "ozaki8, tf32x3, fp64p)")
     args = ap.parse_args()
     if args.warmup < 3 and args.workload in ("dmrg", "c1", "tdvp", "qn"):
         raise SystemExit("warmup must be >= 3")

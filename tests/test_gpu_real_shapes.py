@@ -1,0 +1,83 @@
+"""Parity against the oracle at the configurations' own shapes (not reduced ones).
+
+* The large 2-site DMRG configuration (Heisenberg N=100, random MPS bond dimension 32
+  from seed 1, maxdim schedule [64, 128, 256, 512, 1024], cutoff 1e-12, densitymatrix
+  expansion, Lanczos krylovdim 3 / maxiter 1) over its first three sweeps (maxdim 64,
+  128, 256), region by region: energies within 1e-10 relative and truncated bond
+  dimensions exactly equal, in the plain FP64 form and in the split-precision form.
+* 2-site TDVP on the depth-5 binary-tree TFIM (63 sites, h = 1, all-up start, dt = 0.05,
+  maxdim 256, cutoff 1e-9, Krylov exponential tol 1e-12) over two time steps: fidelity
+  with the oracle's state >= 1 - 1e-8 and equal bond dimensions.
+"""
+import numpy as np
+import pytest
+
+import networksolvers_gb300 as ns
+import networksolvers_gb300.models as m
+
+pytestmark = pytest.mark.gpu
+
+C3_KW = dict(nsweeps=3, nsites=2, updater_kwargs=dict(krylovdim=3, maxiter=1),
+             extracter_kwargs=dict(trunc=dict(cutoff=1e-12, maxdim=[64, 128, 256, 512, 1024]),
+                                   subspace_algorithm="densitymatrix"),
+             inserter_kwargs=dict(trunc=dict(cutoff=1e-12, maxdim=[64, 128, 256, 512, 1024])))
+
+
+def _record(run, H, psi0, **kw):
+    rec = []
+
+    def cb(prob, sweep, region, which, **k):
+        rec.append((sweep, which, prob.eigenvalue, prob.last_insert.get("newdim", -1),
+                    prob.last_insert.get("truncerr", 0.0)))
+
+    E, psi = run(H, psi0, region_callback=cb, **kw)
+    return E, np.array(rec)
+
+
+@pytest.fixture(scope="module")
+def c3_oracle():
+    from oracle import sweep as osw
+    H, psi0 = m.heisenberg_chain(100), m.random_state(m.chain_graph(100), 32, seed=1)
+    E, rec = _record(osw.dmrg, H, psi0, **C3_KW)
+    return H, psi0, E, rec
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_c3_first_three_sweeps_match_oracle(nsg_ctx, c3_oracle, precision):
+    H, psi0, Eo, ro = c3_oracle
+    nsg_ctx.set_precision(precision)
+    try:
+        E, r = _record(ns.dmrg, H, psi0, **C3_KW)
+    finally:
+        nsg_ctx.set_precision("fp64")
+    assert r.shape == ro.shape
+    assert np.array_equal(r[:, 3], ro[:, 3]), np.nonzero(r[:, 3] != ro[:, 3])[0][:5]
+    rel = np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])
+    assert np.max(rel) < 1e-10, (np.argmax(rel), np.max(rel))
+    assert abs(E - Eo) / abs(Eo) < 1e-10
+
+
+@pytest.mark.parametrize("precision", ["fp64", "ozaki"])
+def test_c2_tree_tdvp_two_steps_matches_oracle(nsg_ctx, precision):
+    from oracle import network as on
+    from oracle import sweep as osw
+    from networksolvers_gb300.models import Network
+    g = m.binary_tree_graph(5)
+    H, psi0 = m.tfim_tree(g, h=1.0).astype(np.complex128), m.all_up_state(g)
+    times = [0.0, 0.05, 0.10]
+    ik = dict(trunc=dict(cutoff=1e-9, maxdim=256))
+    ref = osw.tdvp(H, psi0, times, nsites=2, updater_kwargs=dict(solver=osw.exponentiate_solver, tol=1e-12),
+                   inserter_kwargs=ik)
+    nsg_ctx.set_precision(precision)
+    try:
+        psi = ns.tdvp(H, psi0, times, nsites=2, updater_kwargs=dict(solver=ns.exponentiate_solver, tol=1e-12),
+                      inserter_kwargs=ik)
+    finally:
+        nsg_ctx.set_precision("fp64")
+    arrs = psi.to_numpy(psi0)
+    net = Network(psi0.graph, arrs, psi0.legs, np.complex128, {"kind": "state"})
+    sites = {v: [i for i in ref[v].inds if i.tags.startswith("Site")][0] for v in ref.g.vertices}
+    got, _ = on.from_network(net, site_index=sites)
+    fid = abs(on.inner(ref, got)) ** 2 / (abs(on.inner(ref, ref)) * abs(on.inner(got, got)))
+    assert fid > 1 - 1e-8, fid
+    assert sorted(ref.linkdims().values()) == sorted(psi.linkdims().values())
