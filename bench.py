@@ -714,6 +714,50 @@ def run_serve(args):
           max_rel_dE_vs_sequential=max(same) if same else None)
 
 
+def run_serve_sweep(args):
+    """The serving mix (see run_serve) offered at increasing Poisson rates (--rates), a
+    fixed number of requests (--requests) per rate, so each rate's arrival window is
+    requests / rate seconds.  Per rate: achieved solves/s, p50 / p99 latency, mean and
+    largest queue wait (admission delay), against the configured 200 req/s.  The
+    sustainable rate is the largest offered rate whose achieved throughput keeps up (at
+    least 90 % of the offered rate) with a queue wait below one median service time.
+    Beside it: sequential plain FP64 solves of the first --sample requests of the
+    lowest rate."""
+    from networksolvers_gb300 import batch
+    rates = [float(r) for r in args.rates.split(",") if r]
+    rows = []
+    seq_rate = None
+    for k, rate in enumerate(rates):
+        jobs = _serve_jobs(rate, args.requests / rate, args.seed + k)
+        if k == 0 and args.sample > 0:
+            t0 = time.perf_counter()
+            batch.SolvePool(workers=1, precision="fp64").run(
+                [batch.Job(j.kind, j.H, j.psi0, j.kwargs, j.tag, 0.0) for j in jobs[:args.sample]])
+            seq_rate = args.sample / (time.perf_counter() - t0)
+        res = batch.SolvePool(workers=args.workers, precision=args.precision).run(jobs)
+        summ = batch.latency_summary(res)
+        ok = [r for r in res if r.error is None]
+        waits = np.array([r.start - r.arrival for r in ok]) if ok else np.zeros(1)
+        service = np.array([r.finish - r.start for r in ok]) if ok else np.zeros(1)
+        rows.append({"offered_per_s": rate, "requests": len(jobs), "achieved_per_s": summ["solves_per_s"],
+                     "p50_s": summ["p50_s"], "p99_s": summ["p99_s"], "mean_wait_s": float(np.mean(waits)),
+                     "max_wait_s": float(np.max(waits)), "median_service_s": float(np.median(service)),
+                     "failed": summ["failed"]})
+        print(json.dumps({"progress": rows[-1]}), file=sys.stderr, flush=True)
+    sustainable = None
+    for r in rows:
+        if r["achieved_per_s"] and r["achieved_per_s"] >= 0.9 * r["offered_per_s"] and \
+                r["mean_wait_s"] < r["median_service_s"]:
+            sustainable = r["offered_per_s"]
+    peak = max((r["achieved_per_s"] or 0.0) for r in rows)
+    _line(metric="served_solves_per_s", value=peak, unit="solves/s", steps=len(rows), warmup=0,
+          ms_per_step=None, dtype=f"f64/c128 ({args.precision})",
+          config={"workload": "serve_xxz_dmrg_tfim_tdvp_mix", "configured_rate_per_s": 200.0, "rates": rates,
+                  "requests_per_rate": args.requests, "workers": args.workers},
+          rates=rows, sustainable_rate_per_s=sustainable,
+          sequential_fp64={"value": seq_rate, "unit": "solves/s", "sample": f"first {args.sample} requests"})
+
+
 def run_qn(args):
     """U(1) block-sparse DMRG (the `conserve_qns=true` path): Heisenberg chain N=40 from the
     Neel state, 2-site, maxdim [32, 64, 128, 256] then 256, cutoff 1e-10, Lanczos krylovdim
@@ -782,7 +826,7 @@ def main():
     ap.add_argument("--precision", default="ozaki", choices=["ozaki", "tf32x3", "fp64"])
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve", "accuracy", "qn"],
+    ap.add_argument("--workload", default="dmrg", choices=["dmrg", "c1", "tdvp", "batch", "serve", "serve_sweep", "accuracy", "qn"],
                     help="dmrg: the N=100 benchmark (default); c1: the N=20 chain; tdvp: binary-tree TFIM "
                          "TDVP; batch: 256 J1-J2 chains on a solve pool; serve: Poisson request stream; "
                          "qn: U(1) block-sparse DMRG")
@@ -792,6 +836,8 @@ def main():
     ap.add_argument("--rate", type=float, default=1.0)
     ap.add_argument("--duration", type=float, default=30.0)
     ap.add_argument("--seed", type=int, default=0)
+    ap.add_argument("--rates", default="0.25,0.5,1,2,4", help="serve_sweep: offered request rates")
+    ap.add_argument("--requests", type=int, default=24, help="serve_sweep: requests per rate")
     ap.add_argument("--sweeps", type=int, default=10)
     ap.add_argument("--forms", default="fp64,ozaki", help="accuracy workload: forms to run (fp64, ozaki, "
                                                           "ozaki8, tf32x3, fp64p)")
@@ -810,6 +856,8 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "serve_sweep":
+        run_serve_sweep(args)
     elif args.workload == "qn":
         run_qn(args)
     else:

@@ -4,7 +4,7 @@ Public API (same names as NetworkSolvers.jl): `dmrg`/`eigsolve`, `tdvp`/`applyex
 the plugins `extracter`, `updater_eigsolve`, `updater_applyexp`, `inserter`,
 `subspace_expand`, the local solvers `eigsolve_solver`, `exponentiate_solver`,
 `runge_kutta_solver`, the region plans, the fused chain `region_step`, `OpSum` /
-`chain_mpo` for Hamiltonians, `batch.SolvePool` for many concurrent solves, and the
+`chain_mpo` / `ttn_operator` for Hamiltonians on chains and trees, `batch.SolvePool` for many concurrent solves, and the
 U(1) block-sparse layer `qn` (`qn_dmrg_chain`, block tensors) for conserve_qns runs.  The
 numerics run in libnsg.so (include/nsg.h); `build_library()` compiles it for sm_103a.
 """
@@ -17,7 +17,7 @@ from .sweep import (dmrg, eigsolve, tdvp, applyexp, extracter, inserter, subspac
 from .network import (euler_tour_edges, euler_tour_vertices, euler_sweep, post_order_dfs_plan,
                       tdvp_regions, tdvp_sub_time_steps, TTN, ProjTTN, LinearMap, inner)
 from ._native import Context, default_context, set_default_context, set_thread_context, NsgError
-from .models import OpSum, chain_mpo
+from .models import OpSum, chain_mpo, ttn_operator
 from . import qn
 from .qn import qn_dmrg_chain
 

@@ -316,7 +316,8 @@ SITE_OPS = {"Sz": SZ, "S+": SP, "S-": SM, "Sx": 0.5 * PX, "Id": ID2, "X": PX, "Z
 class OpSum:
     """A sum of products of on-site operators, written as in ITensors:
     `os.add(coef, "Sz", i, "Sz", j)` or `os += (coef, "S+", i, "S-", j)`.  Operators are
-    names of SITE_OPS (S=1/2 basis order Up, Dn) or d x d arrays; sites are 1-based."""
+    names of SITE_OPS (S=1/2 basis order Up, Dn) or d x d arrays; sites are 1-based
+    integers on a chain and vertex names (any hashable) on a tree."""
 
     def __init__(self):
         self.terms = []
@@ -326,7 +327,9 @@ class OpSum:
             raise ValueError("OpSum.add(coef, op1, site1, op2, site2, ...)")
         factors = []
         for k in range(0, len(ops), 2):
-            op, site = ops[k], int(ops[k + 1])
+            op, site = ops[k], ops[k + 1]
+            if isinstance(site, (int, np.integer)):
+                site = int(site)
             mat = SITE_OPS[op] if isinstance(op, str) else np.asarray(op)
             factors.append((site, mat))
         self.terms.append((coef, factors))
@@ -402,6 +405,118 @@ def chain_mpo(opsum, n, d=2):
             tensors[j] = np.ascontiguousarray(W)
             legs[j] = [('w', el), ('sp', j), ('s', j), ('w', er)]
     return Network(g, tensors, legs, dt, {"kind": "operator", "w": max(bdim.values()) if bdim else 1})
+
+
+def ttn_operator(opsum, graph, root=None, d=2):
+    """Exact tree operator (TTN) of an OpSum on a tree graph: the finite-state
+    construction of `chain_mpo` on a rooted tree (the input format `itn.ttn(os, sites)` of
+    the reference's tests, e.g. test_tree_dmrg.jl:28).
+
+    Rooted at `root` (default: the last vertex), every edge (child c, parent p) carries
+    the automaton state of the subtree below it: IDENT (identity everywhere below),
+    DONE (exactly one term completed below) or, for each term whose support lies partly
+    below and partly above the edge, that term's private state.  Link dimension = 2 +
+    the number of terms crossing the edge (5 on every edge of a nearest-neighbour
+    Heisenberg tree).  A vertex tensor sends: all children IDENT -> IDENT (identity);
+    one child DONE, the others IDENT -> DONE (identity); and, for each term with support
+    in its subtree that does not lie below a single child, the children holding part of
+    the term in that term's state, the others IDENT, to the term's state (the term
+    continues above) or to DONE (the vertex is the term's topmost vertex, where the
+    coefficient is applied), with the term's operator at the vertex (identity when the
+    vertex only joins parts of the support).  The root keeps only the DONE output.
+    Operators of one term on the same vertex multiply in the order given."""
+    verts = list(graph.vertices)
+    if root is None:
+        root = verts[-1]
+    parent = {root: None}
+    order = [root]
+    k = 0
+    while k < len(order):
+        v = order[k]
+        for u in graph.neighbors(v):
+            if u not in parent:
+                parent[u] = v
+                order.append(u)
+        k += 1
+    if len(order) != len(verts):
+        raise ValueError("ttn_operator: the graph is not a connected tree")
+    children = {v: [u for u in graph.neighbors(v) if parent.get(u) == v] for v in verts}
+    below = {}
+    for v in reversed(order):  # leaves first
+        sset = {v}
+        for c_ in children[v]:
+            sset |= below[c_]
+        below[v] = sset
+    cplx = any(np.iscomplexobj(m_) or np.iscomplexobj(c_) for c_, fs in opsum.terms for _, m_ in fs)
+    dt = np.complex128 if cplx else np.float64
+    ident = np.eye(d, dtype=dt)
+    terms = []
+    for c_, fs in opsum.terms:
+        per = {}
+        for site, mat in fs:
+            if site not in parent:
+                raise ValueError(f"OpSum site {site!r} is not a vertex of the graph")
+            per[site] = per[site] @ mat if site in per else np.asarray(mat, dtype=dt)
+        terms.append((c_, per, set(per)))
+    IDENT, DONE = 0, 1
+    # private states: edge (c -> parent) for every term crossing it
+    state, wdim = {}, {}
+    for v in verts:
+        if parent[v] is None:
+            continue
+        kk = 2
+        for t, (_, _, sup) in enumerate(terms):
+            if sup & below[v] and not sup <= below[v]:
+                state[(t, v)] = kk
+                kk += 1
+        wdim[v] = kk
+    tensors, legs = {}, {}
+    for v in verts:
+        p, ch = parent[v], children[v]
+        shape = ([wdim[v]] if p is not None else []) + [wdim[c_] for c_ in ch] + [d, d]
+        W = np.zeros(shape, dtype=dt)
+
+        def put(pstate, cstates, op):
+            if p is None and pstate != DONE:
+                return
+            idx = ([pstate] if p is not None else []) + list(cstates)
+            W[tuple(idx)] += op
+
+        zero = [IDENT] * len(ch)
+        put(IDENT, zero, ident)
+        for i in range(len(ch)):
+            cs = list(zero)
+            cs[i] = DONE
+            put(DONE, cs, ident)
+        for t, (coef, per, sup) in enumerate(terms):
+            if not sup & below[v]:
+                continue
+            if any(sup <= below[c_] for c_ in ch):
+                continue  # the term completes inside one child's subtree
+            cs = [state[(t, c_)] if sup & below[c_] else IDENT for c_ in ch]
+            op = per.get(v, ident)
+            if sup <= below[v]:
+                put(DONE, cs, coef * op)
+            else:
+                put(state[(t, v)], cs, op)
+        # stored leg order [first link, s', s, other links] (permute_indices.jl:4-18)
+        internal = ([('w', graph.edge_key(v, p))] if p is not None else []) + \
+                   [('w', graph.edge_key(v, c_)) for c_ in ch] + [('sp', v), ('s', v)]
+        target = _permuted_legs(graph, v, 'w', [('sp', v), ('s', v)])
+        perm = [internal.index(l_) for l_ in target]
+        tensors[v] = np.ascontiguousarray(W.transpose(perm))
+        legs[v] = target
+    return Network(graph, tensors, legs, dt, {"kind": "operator", "w": max(wdim.values()) if wdim else 1})
+
+
+def heisenberg_opsum(graph, J=1.0, delta=1.0):
+    """The OpSum of test_tree_dmrg.jl:21-27: Σ_edges J (Δ Sz Sz + ½ S+ S- + ½ S- S+)."""
+    os_ = OpSum()
+    for (u, v) in graph.edges:
+        os_.add(J * delta, "Sz", u, "Sz", v)
+        os_.add(0.5 * J, "S+", u, "S-", v)
+        os_.add(0.5 * J, "S-", u, "S+", v)
+    return os_
 
 
 def heisenberg_chain(n, J=1.0):

@@ -3,8 +3,14 @@
 * The large 2-site DMRG configuration (Heisenberg N=100, random MPS bond dimension 32
   from seed 1, maxdim schedule [64, 128, 256, 512, 1024], cutoff 1e-12, densitymatrix
   expansion, Lanczos krylovdim 3 / maxiter 1) over its first three sweeps (maxdim 64,
-  128, 256), region by region: energies within 1e-10 relative and truncated bond
-  dimensions exactly equal, in the plain FP64 form and in the split-precision form.
+  128, 256), region by region, in the plain FP64 form and in the split-precision form:
+  energies within 1e-10 relative and truncated bond dimensions exactly equal up to the
+  first region whose truncation is a cutoff tie.  At a tie the discarded weight of the
+  oracle's decision lies within 1e-14 (relative to the total weight) of the cutoff, below
+  what an FP64 singular-value computation resolves, so either count is correct and from
+  there the two runs follow different (equally valid) trajectories; the final energies
+  then agree to 1e-8 (a plain run from a start perturbed by 1e-13 moves the 10-sweep
+  energy of this configuration by 7e-10).
 * 2-site TDVP on the depth-5 binary-tree TFIM (63 sites, h = 1, all-up start, dt = 0.05,
   maxdim 256, cutoff 1e-9, Krylov exponential tol 1e-12) over two time steps: fidelity
   with the oracle's state >= 1 - 1e-8 and equal bond dimensions.
@@ -51,10 +57,21 @@ def test_c3_first_three_sweeps_match_oracle(nsg_ctx, c3_oracle, precision):
     finally:
         nsg_ctx.set_precision("fp64")
     assert r.shape == ro.shape
-    assert np.array_equal(r[:, 3], ro[:, 3]), np.nonzero(r[:, 3] != ro[:, 3])[0][:5]
-    rel = np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])
+    diff = np.nonzero(r[:, 3] != ro[:, 3])[0]
+    upto = int(diff[0]) if len(diff) else len(r)
+    rel = np.abs(r[:upto, 2] - ro[:upto, 2]) / np.abs(ro[:upto, 2])
     assert np.max(rel) < 1e-10, (np.argmax(rel), np.max(rel))
-    assert abs(E - Eo) / abs(Eo) < 1e-10
+    if len(diff):
+        cutoff = 1e-12
+        # the first differing count is a cutoff tie: one of the two decisions sits within
+        # 1e-14 of the cutoff (discarded weight relative to the total weight)
+        margin = min(abs(ro[upto, 4] - cutoff), abs(r[upto, 4] - cutoff))
+        assert margin < 1e-14, (upto, r[upto], ro[upto])
+        assert abs(int(r[upto, 3]) - int(ro[upto, 3])) == 1
+        assert upto > 400, upto  # sweeps 1-2 and the start of sweep 3 agree exactly
+        assert abs(E - Eo) / abs(Eo) < 1e-8
+    else:
+        assert abs(E - Eo) / abs(Eo) < 1e-10
 
 
 @pytest.mark.parametrize("precision", ["fp64", "ozaki"])

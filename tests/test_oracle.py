@@ -153,3 +153,78 @@ def test_opsum_chain_mpo_matches_dense_sums():
     os_.add(0.3, "S+", 2, "S-", 2, "Sz", 4)  # two operators on one site multiply in order
     ref += 0.3 * _kron_term(n, [(2, m.SP @ m.SM), (4, m.SZ)])
     assert np.allclose(_dense(m.chain_mpo(os_, n)), ref, atol=1e-12)
+
+
+def _dense_seq(H):
+    """Dense matrix of an operator network, contracted vertex by vertex in vertex order
+    (an exhaustive contraction-order search is too slow for ten tensors)."""
+    (g, T), sites = network.from_network(H)
+    acc = None
+    for v in g.vertices:
+        acc = T[v] if acc is None else acc * T[v]
+    bra = [sites[v].prime() for v in g.vertices]
+    ket = [sites[v] for v in g.vertices]
+    d = 2 ** len(g.vertices)
+    return acc.permute(bra + ket).data.reshape(d, d)
+
+
+def _kron_tree(vertices, factors):
+    pos = {v: k for k, v in enumerate(vertices)}
+    mats = [np.eye(2, dtype=complex) for _ in vertices]
+    for site, mat in factors:
+        mats[pos[site]] = mats[pos[site]] @ mat
+    out = np.array([[1.0 + 0j]])
+    for mt in mats:
+        out = np.kron(out, mt)
+    return out
+
+
+def test_opsum_ttn_operator_matches_dense_sums():
+    """OpSum -> tree operator (finite-state construction on a rooted tree) against the
+    dense sum of Kronecker products: the Heisenberg OpSum of test_tree_dmrg.jl:21-27 on
+    the 10-site three-branch tree (equal to the hand-built tree operator, link dimension
+    5, for every choice of root), and random 1-, 2- and 3-site terms, including two
+    operators on one vertex and a complex coefficient, on a 7-site binary tree."""
+    g = m.build_tree_graph(3, 3)
+    ref = _dense_seq(m.heisenberg_tree(g))
+    for root in (None, (0, 0), (2, 3)):
+        H = m.ttn_operator(m.heisenberg_opsum(g), g, root=root)
+        assert max(max(t.shape) for t in H.tensors.values()) == 5
+        assert np.allclose(_dense_seq(H), ref, atol=1e-13)
+    g = m.binary_tree_graph(2)
+    rng = np.random.default_rng(7)
+    os_ = m.OpSum()
+    dense = np.zeros((2 ** 7, 2 ** 7), dtype=complex)
+    names = ["Sz", "S+", "S-", "Sx", "Sy", "X", "Z", "N"]
+    for _ in range(14):
+        k = int(rng.integers(1, 4))
+        sites = [g.vertices[i] for i in rng.choice(len(g.vertices), size=k, replace=False)]
+        ops = [names[int(rng.integers(len(names)))] for _ in sites]
+        c = float(rng.standard_normal())
+        args = []
+        for o, s_ in zip(ops, sites):
+            args += [o, s_]
+        os_.add(c, *args)
+        dense += c * _kron_tree(g.vertices, [(s_, m.SITE_OPS[o]) for o, s_ in zip(ops, sites)])
+    os_.add(0.25 - 0.5j, "S+", 3, "S-", 3, "Z", 6)
+    dense += (0.25 - 0.5j) * _kron_tree(g.vertices, [(3, m.SP @ m.SM), (6, m.PZ)])
+    for root in (None, 0, 4):
+        H = m.ttn_operator(os_, g, root=root)
+        assert np.allclose(_dense_seq(H), dense, atol=1e-12)
+    # on a chain it is the chain MPO's operator
+    n = 5
+    osc = m.OpSum()
+    for j in range(1, n):
+        osc.add(0.7, "Sz", j, "Sz", j + 1)
+        osc.add(0.3, "X", j)
+    assert np.allclose(_dense_seq(m.ttn_operator(osc, m.chain_graph(n))), _dense_seq(m.chain_mpo(osc, n)), atol=1e-13)
+
+
+def test_opsum_ttn_tree_dmrg_vs_ed():
+    """test_tree_dmrg.jl:18-53 with the operator built from the OpSum (itn.ttn(os, s),
+    test_tree_dmrg.jl:28): 2-site DMRG on the three-branch tree within 1e-5 of ED."""
+    g = m.build_tree_graph(3, 3)
+    H = m.ttn_operator(m.heisenberg_opsum(g), g)
+    E, _ = sweep.dmrg(H, m.neel_state(g), nsweeps=5, nsites=2,
+                      inserter_kwargs=dict(trunc=dict(cutoff=1e-5, maxdim=40)))
+    assert abs(E - _ed_heis(g)) < 1e-5
