@@ -187,6 +187,60 @@ __global__ void __launch_bounds__(kThreads) multi_axpy_kernel(int64_t n, int nv,
   }
 }
 
+// multi_axpy with coefficients read from device memory, scaled by `sign` (+1 or -1:
+// exact), in the arithmetic of multi_axpy_kernel
+template <bool CPLX>
+__global__ void __launch_bounds__(kThreads)
+    multi_axpy_devcoef_kernel(int64_t n, int nv, VecPtrs vp, const double* __restrict__ coef, double sign, void* w_) {
+  __shared__ double cs[128];
+  for (int j = threadIdx.x; j < 2 * nv; j += blockDim.x) cs[j] = sign * coef[j];
+  __syncthreads();
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    if constexpr (CPLX) {
+      double2* w = (double2*)w_;
+      double2 acc = w[i];
+      for (int j = 0; j < nv; ++j) {
+        double2 a = ((const double2*)vp.v[j])[i];
+        double cr = cs[2 * j], ci = cs[2 * j + 1];
+        acc.x = fma(cr, a.x, fma(-ci, a.y, acc.x));
+        acc.y = fma(cr, a.y, fma(ci, a.x, acc.y));
+      }
+      w[i] = acc;
+    } else {
+      double* w = (double*)w_;
+      double acc = w[i];
+      for (int j = 0; j < nv; ++j) acc = fma(cs[2 * j], ((const double*)vp.v[j])[i], acc);
+      w[i] = acc;
+    }
+  }
+}
+
+// y = a x + b y with a, b from a device sum of squares s (in the arithmetic of the
+// axpby kernels): mode 0: a = 1 / sqrt(s), b = 0 (normalise); mode 1: a = -sqrt(s), b = 1
+template <bool CPLX>
+__global__ void axpby_devscalar_kernel(int64_t n, const double* __restrict__ s_dev, int mode, const void* x_, void* y_) {
+  const double nr = sqrt(s_dev[0]);
+  const double a = mode == 0 ? 1.0 / nr : -nr;
+  const double b = mode == 0 ? 0.0 : 1.0;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n; i += int64_t(gridDim.x) * blockDim.x) {
+    if constexpr (CPLX) {
+      const double2* x = (const double2*)x_;
+      double2* y = (double2*)y_;
+      double2 ax = cmul(make_double2(a, 0.0), x[i]);
+      if (b != 0.0) {
+        double2 by = cmul(make_double2(b, 0.0), y[i]);
+        ax.x += by.x;
+        ax.y += by.y;
+      }
+      y[i] = ax;
+    } else {
+      const double* x = (const double*)x_;
+      double* y = (double*)y_;
+      y[i] = (b == 0.0 ? a * x[i] : fma(a, x[i], b * y[i]));
+    }
+  }
+}
+
 template <typename T>
 __global__ void copy_columns_kernel(int64_t rows, int64_t ncols, const T* __restrict__ src, int64_t lds,
                                     const int* __restrict__ colidx, T* __restrict__ dst, int64_t ldd) {
@@ -364,6 +418,47 @@ void multi_axpy(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, 
     multi_axpy_kernel<false><<<grid, kThreads, 0, c->stream>>>(n, nv, p, w);
   count_launch(c);
   check_launch("multi_axpy");
+}
+
+void multi_dot_dev(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, const void* w, double* out_dev) {
+  NSG_CHECK(nv >= 1 && nv <= 64, NSG_ERR_INVALID, "multi_dot: 1..64 vectors");
+  int nb = grid_for(c, n, 2);
+  if (nb > 256) nb = 256;
+  double* scratch = dev_scratch(c, size_t(2) * nb * nv);
+  VecPtrs vp;
+  for (int j = 0; j < nv; ++j) vp.v[j] = v[j];
+  dim3 grid(nb, nv);
+  if (dtype == NSG_C128)
+    dot_partial_kernel<true><<<grid, kThreads, 0, c->stream>>>(n, vp, w, scratch);
+  else
+    dot_partial_kernel<false><<<grid, kThreads, 0, c->stream>>>(n, vp, w, scratch);
+  dot_final_kernel<<<nv, 32, 0, c->stream>>>(nb, scratch, out_dev);
+  count_launch(c, 2);
+  check_launch("multi_dot_dev");
+}
+
+void multi_axpy_devcoef(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, const double* coef_dev,
+                        double sign, void* w) {
+  NSG_CHECK(nv >= 1 && nv <= 64, NSG_ERR_INVALID, "multi_axpy: 1..64 vectors");
+  VecPtrs vp;
+  for (int j = 0; j < nv; ++j) vp.v[j] = v[j];
+  int grid = grid_for(c, n);
+  if (dtype == NSG_C128)
+    multi_axpy_devcoef_kernel<true><<<grid, kThreads, 0, c->stream>>>(n, nv, vp, coef_dev, sign, w);
+  else
+    multi_axpy_devcoef_kernel<false><<<grid, kThreads, 0, c->stream>>>(n, nv, vp, coef_dev, sign, w);
+  count_launch(c);
+  check_launch("multi_axpy_devcoef");
+}
+
+void axpby_devscalar(nsg_ctx* c, int dtype, int64_t n, const double* s_dev, int mode, const void* x, void* y) {
+  int grid = grid_for(c, n);
+  if (dtype == NSG_C128)
+    axpby_devscalar_kernel<true><<<grid, kThreads, 0, c->stream>>>(n, s_dev, mode, x, y);
+  else
+    axpby_devscalar_kernel<false><<<grid, kThreads, 0, c->stream>>>(n, s_dev, mode, x, y);
+  count_launch(c);
+  check_launch("axpby_devscalar");
 }
 
 double norm2(nsg_ctx* c, int dtype, int64_t n, const void* x) {

@@ -184,6 +184,7 @@ __global__ void slice_kernel(const double* __restrict__ src, int64_t rows, int64
 struct OzEpi {
   double* C;
   int64_t ldc, sC, M, N;
+  int64_t crs;  // stride between rows of C in doubles (1, or 2 for one part of complex C)
   double alpha, beta;
   const double* sa;  // row scales of A  [batch_a][Mp]
   const double* sb;  // row scales of B^T [batch_b][Np]
@@ -401,7 +402,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int kb = pow2_exponent(ep.sb[(ep.b_batched ? bz : 0) * ep.Np + col]);
             double v = scale_pow2(widen(hi[j]) + widen(lo[j]), ka + kb);
             if (!unit_alpha) v *= ep.alpha;
-            double* cp = ep.C + bz * ep.sC + row + col * ep.ldc;
+            double* cp = ep.C + bz * ep.sC + row * ep.crs + col * ep.ldc;
             *cp = (ep.beta == 0.0) ? v : fma(ep.beta, *cp, v);
           }
         }
@@ -463,39 +464,97 @@ void slice_operand(nsg_ctx* c, const double* src, int64_t rows, int64_t K, int64
   check_launch("ozaki slices");
 }
 
+// One operand of an Ozaki product, sliced: S bf16 slices [batch][S][rows_p][K_p] and the
+// power-of-two row scales [batch][rows_p].
+struct OzOperand {
+  __nv_bfloat16* slices = nullptr;
+  double* scales = nullptr;
+  int64_t rows_p = 0, batch = 1;
+};
+
 template <int S>
-bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
+size_t oz_operand_bytes(int64_t rows_p, int64_t K_p, int64_t batch) {
+  return ((2 * size_t(S) * rows_p * K_p * batch + 255) & ~size_t(255)) + ((8 * size_t(rows_p) * batch + 255) & ~size_t(255));
+}
+
+// slices of op(X) viewed as rows x K (element (r, k) at src[b bs + r rs + k ks], in doubles)
+template <int S>
+OzOperand oz_prepare(nsg_ctx* c, unsigned char* mem, const double* src, int64_t rows, int64_t K, int64_t rs,
+                     int64_t ks, int64_t bs, int64_t batch, int64_t rows_p, int64_t K_p) {
+  OzOperand o;
+  o.slices = (__nv_bfloat16*)mem;
+  o.scales = (double*)(mem + ((2 * size_t(S) * rows_p * K_p * batch + 255) & ~size_t(255)));
+  o.rows_p = rows_p;
+  o.batch = batch;
+  slice_operand<S>(c, src, rows, K, rs, ks, bs, batch, rows_p, K_p, o.scales, o.slices);
+  return o;
+}
+
+// C (+)= alpha A B^T-form product of two prepared operands into C (stride ldc between
+// columns, sC between batch entries, crs between rows; all in doubles)
+template <int S>
+void oz_product(nsg_ctx* c, const OzOperand& A, const OzOperand& B, int64_t M, int64_t N, int64_t K_p, int64_t batch,
+                double* C, int64_t ldc, int64_t sC, int64_t crs, double alpha, double beta, int64_t flop_k) {
   constexpr int SMEM_BYTES = Oz<S>::SMEM_BYTES;
-  if (g.dtype != NSG_F64) return false;
-  if (g.opA == OP_C || g.opA == OP_R || g.opB == OP_C || g.opB == OP_R) return false;
-  if (g.M < 64 || g.N < 32 || g.K < 64) return false;
-  if (g.batch > 65535) return false;
-  const int64_t Mp = (g.M + BM - 1) / BM * BM, Np = (g.N + BN - 1) / BN * BN, Kp = (g.K + BKS - 1) / BKS * BKS;
-  const int64_t ars = (g.opA == OP_N) ? 1 : g.lda, aks = (g.opA == OP_N) ? g.lda : 1;
-  const int64_t brs = (g.opB == OP_N) ? g.ldb : 1, bks = (g.opB == OP_N) ? 1 : g.ldb;
-  const int64_t ab = (g.strideA == 0) ? 1 : g.batch, bb = (g.strideB == 0) ? 1 : g.batch;
-  size_t nA = size_t(S) * Mp * Kp * ab, nB = size_t(S) * Np * Kp * bb;
-  size_t bytes = 2 * (nA + nB) + 8 * (size_t(Mp) * ab + size_t(Np) * bb) + 256;
-  ScopedBuf sbuf(c, bytes);
-  unsigned char* buf = (unsigned char*)sbuf.p;
-  __nv_bfloat16* As = (__nv_bfloat16*)buf;
-  __nv_bfloat16* Bs = As + nA;
-  double* sa = (double*)(((uintptr_t)(Bs + nB) + 255) & ~(uintptr_t)255);
-  double* sb = sa + Mp * ab;
-  slice_operand<S>(c, (const double*)g.A, g.M, g.K, ars, aks, g.strideA, ab, Mp, Kp, sa, As);
-  slice_operand<S>(c, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp, sb, Bs);
-  CUtensorMap mA = make_map(As, Mp, Kp, S * ab, BM, S), mB = make_map(Bs, Np, Kp, S * bb, BN, S);
+  CUtensorMap mA = make_map(A.slices, A.rows_p, K_p, S * A.batch, BM, S),
+              mB = make_map(B.slices, B.rows_p, K_p, S * B.batch, BN, S);
   int* err = device_flag(c);  // checked once at the end of the public call
   ensure_smem_limit((const void*)oz_gemm_kernel<S>, SMEM_BYTES);
-  OzEpi ep{(double*)g.C, g.ldc, g.strideC, g.M, g.N, g.alpha_re, g.beta_re, sa, sb, Mp, Np,
-           ab > 1, bb > 1, err};
-  dim3 grid(unsigned(Mp / BM), unsigned(Np / BN), unsigned(g.batch));
+  OzEpi ep{C, ldc, sC, M, N, crs, alpha, beta, A.scales, B.scales, A.rows_p, B.rows_p, A.batch > 1, B.batch > 1, err};
+  dim3 grid(unsigned(A.rows_p / BM), unsigned(B.rows_p / BN), unsigned(batch));
   {
-    ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(g.M) * double(g.N) * double(g.K) * double(g.batch));
-    oz_gemm_kernel<S><<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, int(Kp / BKS), ep);
+    ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(M) * double(N) * double(flop_k) * double(batch));
+    oz_gemm_kernel<S><<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, int(K_p / BKS), ep);
   }
   count_launch(c);
   check_launch("oz_gemm");
+}
+
+template <int S>
+bool gemm_ozaki_impl(nsg_ctx* c, const GemmArgs& g) {
+  if (g.dtype != NSG_F64 && g.dtype != NSG_C128) return false;
+  if (g.M < 64 || g.N < 32 || g.K < 64) return false;
+  if (g.batch > 65535) return false;
+  const bool cplx = g.dtype == NSG_C128;
+  if (!cplx && (g.opA == OP_C || g.opA == OP_R || g.opB == OP_C || g.opB == OP_R)) return false;
+  // complex: real scalars only (the four real products carry the signs)
+  if (cplx && (g.alpha_im != 0.0 || g.beta_im != 0.0)) return false;
+  const int64_t Mp = (g.M + BM - 1) / BM * BM, Np = (g.N + BN - 1) / BN * BN, Kp = (g.K + BKS - 1) / BKS * BKS;
+  const bool transA = g.opA == OP_T || g.opA == OP_C, transB = g.opB == OP_T || g.opB == OP_C;
+  const int64_t ars = !transA ? 1 : g.lda, aks = !transA ? g.lda : 1;
+  const int64_t brs = !transB ? g.ldb : 1, bks = !transB ? 1 : g.ldb;
+  const int64_t ab = (g.strideA == 0) ? 1 : g.batch, bb = (g.strideB == 0) ? 1 : g.batch;
+  const size_t opA_bytes = oz_operand_bytes<S>(Mp, Kp, ab), opB_bytes = oz_operand_bytes<S>(Np, Kp, bb);
+  if (!cplx) {
+    ScopedBuf sbuf(c, opA_bytes + opB_bytes);
+    unsigned char* buf = (unsigned char*)sbuf.p;
+    OzOperand A = oz_prepare<S>(c, buf, (const double*)g.A, g.M, g.K, ars, aks, g.strideA, ab, Mp, Kp);
+    OzOperand B = oz_prepare<S>(c, buf + opA_bytes, (const double*)g.B, g.N, g.K, brs, bks, g.strideB, bb, Np, Kp);
+    oz_product<S>(c, A, B, g.M, g.N, Kp, g.batch, (double*)g.C, g.ldc, g.strideC, 1, g.alpha_re, g.beta_re, g.K);
+    return true;
+  }
+  // complex: A = Ar + i sa Ai, B = Br + i sb Bi (sa, sb = -1 for conjugated operands), as
+  // four real products on the interleaved parts (strides doubled, imaginary parts at +1):
+  //   Re C = alpha (Ar Br - sa sb Ai Bi) + beta Re C,  Im C = alpha (sb Ar Bi + sa Ai Br) + beta Im C
+  const double sa = (g.opA == OP_C || g.opA == OP_R) ? -1.0 : 1.0;
+  const double sbs = (g.opB == OP_C || g.opB == OP_R) ? -1.0 : 1.0;
+  ScopedBuf sbuf(c, 2 * (opA_bytes + opB_bytes));
+  unsigned char* buf = (unsigned char*)sbuf.p;
+  const double* Ad = (const double*)g.A;
+  const double* Bd = (const double*)g.B;
+  OzOperand Ar = oz_prepare<S>(c, buf, Ad, g.M, g.K, 2 * ars, 2 * aks, 2 * g.strideA, ab, Mp, Kp);
+  OzOperand Ai = oz_prepare<S>(c, buf + opA_bytes, Ad + 1, g.M, g.K, 2 * ars, 2 * aks, 2 * g.strideA, ab, Mp, Kp);
+  OzOperand Br = oz_prepare<S>(c, buf + 2 * opA_bytes, Bd, g.N, g.K, 2 * brs, 2 * bks, 2 * g.strideB, bb, Np, Kp);
+  OzOperand Bi = oz_prepare<S>(c, buf + 2 * opA_bytes + opB_bytes, Bd + 1, g.N, g.K, 2 * brs, 2 * bks,
+                               2 * g.strideB, bb, Np, Kp);
+  double* Cr = (double*)g.C;
+  double* Ci = Cr + 1;
+  const int64_t ldc = 2 * g.ldc, sC = 2 * g.strideC;
+  const double al = g.alpha_re, be = g.beta_re;
+  oz_product<S>(c, Ar, Br, g.M, g.N, Kp, g.batch, Cr, ldc, sC, 2, al, be, g.K);
+  oz_product<S>(c, Ai, Bi, g.M, g.N, Kp, g.batch, Cr, ldc, sC, 2, -sa * sbs * al, 1.0, g.K);
+  oz_product<S>(c, Ar, Bi, g.M, g.N, Kp, g.batch, Ci, ldc, sC, 2, sbs * al, be, g.K);
+  oz_product<S>(c, Ai, Br, g.M, g.N, Kp, g.batch, Ci, ldc, sC, 2, sa * al, 1.0, g.K);
   return true;
 }
 

@@ -158,6 +158,37 @@ void lanczos_step(nsg_ctx* c, nsg_linmap* m, std::vector<nsg_tensor*>& V, int j,
   *beta_j = b;
 }
 
+// The Lanczos steps of one cycle with every scalar kept on the device: the two CGS
+// passes' coefficients and the sum of squares of w stay in `scal` (one block of
+// 4 (j + 1) + 2 doubles per step j, at step_offset(j)) and the next basis vector is
+// normalised by a kernel that reads that sum of squares, so the cycle issues no host
+// synchronisation; the host reads every scalar back once.  The kernels and the operand
+// order are those of lanczos_step, hence the same vectors.  All K steps run; steps after
+// a breakdown are discarded by the caller.
+static size_t step_offset(int j) { return size_t(2) * j * (j + 1) + size_t(2) * j; }  // sum_{i<j} (4 (i+1) + 2)
+void lanczos_cycle_dev(nsg_ctx* c, nsg_linmap* m, std::vector<nsg_tensor*>& V, int K, nsg_tensor* w, double* scal) {
+  const int dt = w->dtype;
+  const int64_t n = w->size;
+  std::vector<const void*> ptrs;
+  for (int j = 0; j < K; ++j) {
+    double* blk = scal + step_offset(j);
+    double* co1 = blk;
+    double* co2 = blk + 2 * (j + 1);
+    double* ss = blk + 4 * (j + 1);
+    linmap_apply(c, m, V[j], w);
+    if (j > 0) axpby_devscalar(c, dt, n, scal + step_offset(j - 1) + 4 * j, 1, V[j - 1]->data, w->data);
+    ptrs.assign(j + 1, nullptr);
+    for (int i = 0; i <= j; ++i) ptrs[i] = V[i]->data;
+    multi_dot_dev(c, dt, n, j + 1, ptrs.data(), w->data, co1);
+    multi_axpy_devcoef(c, dt, n, j + 1, ptrs.data(), co1, -1.0, w->data);
+    multi_dot_dev(c, dt, n, j + 1, ptrs.data(), w->data, co2);
+    multi_axpy_devcoef(c, dt, n, j + 1, ptrs.data(), co2, -1.0, w->data);
+    const void* wp[1] = {w->data};
+    multi_dot_dev(c, dt, n, 1, wp, w->data, ss);
+    if (j + 1 < K) axpby_devscalar(c, dt, n, ss, 0, w->data, V[j + 1]->data);
+  }
+}
+
 }  // namespace
 }  // namespace nsg
 
@@ -178,6 +209,61 @@ int nsg_eigsolve(nsg_ctx* c, nsg_linmap* m, nsg_tensor* x, int krylovdim, int ma
   nsg_tensor* w = store.add(x);
   int ops = 0;
   double lam = 0.0;
+  if (maxiter == 1) {
+    // One cycle (the reference's default, maxiter 1): device-resident scalars and one
+    // host read.  Falls through to the synchronous form below when the start vector's or
+    // a kept step's sum of squares leaves the range where sqrt(sum) is exact enough
+    // (the synchronous norm rescales there) -- the same arithmetic otherwise.
+    const size_t nscal = step_offset(krylovdim) + 2;
+    ScopedBuf sb(c, sizeof(double) * nscal);
+    double* scal = (double*)sb.p;
+    double* sx = scal + step_offset(krylovdim);
+    const void* xp[1] = {x->data};
+    multi_dot_dev(c, dt, n, 1, xp, x->data, sx);
+    axpby_devscalar(c, dt, n, sx, 0, x->data, V[0]->data);
+    lanczos_cycle_dev(c, m, V, krylovdim, w, scal);
+    std::vector<double> hs(nscal);
+    NSG_CUDA(cudaMemcpyAsync(hs.data(), scal, sizeof(double) * nscal, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaStreamSynchronize(c->stream));
+    auto in_range = [](double q) { return std::isfinite(q) && q > 1e-280 && q < 1e280; };
+    bool ok = in_range(hs[step_offset(krylovdim)]);
+    std::vector<double> alpha, beta;
+    int k = 0;
+    for (int j = 0; j < krylovdim && ok; ++j) {
+      const double* blk = hs.data() + step_offset(j);
+      const double a = blk[2 * j] + blk[2 * (j + 1) + 2 * j];
+      const double q = blk[4 * (j + 1)];
+      if (!std::isfinite(a) || !std::isfinite(q)) {
+        ok = false;
+        break;
+      }
+      const double b = std::sqrt(q);
+      alpha.push_back(a);
+      beta.push_back(b);
+      k = j + 1;
+      if (j + 1 == krylovdim || b <= tol) break;
+      if (!in_range(q)) ok = false;
+    }
+    if (ok) {
+      ops = k;
+      std::vector<double> ev(k), Y(size_t(k) * k);
+      tridiag_eig(k, alpha.data(), beta.data(), ev.data(), Y.data());
+      lam = ev[0];
+      std::vector<double> coef(2 * k, 0.0);
+      for (int j = 0; j < k; ++j) coef[2 * j] = Y[j];
+      std::vector<const void*> ptrs(k);
+      for (int j = 0; j < k; ++j) ptrs[j] = V[j]->data;
+      NSG_CUDA(cudaMemsetAsync(x->data, 0, x->bytes, c->stream));
+      multi_axpy(c, dt, n, k, ptrs.data(), coef.data(), x->data);
+      const void* xq[1] = {x->data};
+      multi_dot_dev(c, dt, n, 1, xq, x->data, sx);
+      axpby_devscalar(c, dt, n, sx, 0, x->data, x->data);
+      *eigval = lam;
+      if (numops) *numops = ops;
+      check_device_flag(c);
+      return NSG_OK;
+    }
+  }
   double nx = norm2(c, dt, n, x->data);
   NSG_CHECK(nx > 0 && std::isfinite(nx), NSG_ERR_NONFINITE, "eigsolve: zero or non-finite start vector");
   axpby(c, dt, n, 1.0 / nx, 0.0, x->data, 0.0, 0.0, V[0]->data);
@@ -237,10 +323,6 @@ int nsg_exponentiate(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_te
   cd remaining = t;
   bool done = false;
   for (int it = 0; it < maxiter && !done; ++it) {
-    double beta0 = norm2(c, dt, n, x->data);
-    if (beta0 == 0.0) break;
-    NSG_CHECK(std::isfinite(beta0), NSG_ERR_NONFINITE, "exponentiate: non-finite vector");
-    axpby(c, dt, n, 1.0 / beta0, 0.0, x->data, 0.0, 0.0, V[0]->data);
     std::vector<double> alpha, beta;
     std::vector<cd> E;  // first column of exp(tau T_k)
     double err = INFINITY;
@@ -254,7 +336,71 @@ int nsg_exponentiate(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_te
       std::vector<cd> E2 = expm_small(kk, A);
       col.assign(E2.begin(), E2.begin() + kk);
     };
-    for (int j = 0; j < krylovdim; ++j) {
+    // Speculative device-resident cycle: the number of steps the previous cycle needed
+    // (plus one) runs without host synchronisation, then the host replays the stopping
+    // rule on the read-back scalars.  The vectors are those of the step-by-step form
+    // (same kernels and arithmetic), so a rule that stops within the speculated steps
+    // gives the identical result; a rule that has not stopped continues step by step from
+    // there, and a sum of squares outside the range of an exact square root restarts the
+    // cycle step by step.
+    double beta0 = 0.0;
+    const int spec = std::min(krylovdim, std::max(2, c->krylov_hint + 1));
+    const int ops_before = ops;
+    bool spec_ok = false;  // the stopping rule fired within the speculated steps
+    int resume = 0;        // > 0: steps 0..resume-1 are valid, continue from step `resume`
+    {
+      const size_t nscal = step_offset(spec) + 2;
+      ScopedBuf sb(c, sizeof(double) * nscal);
+      double* scal = (double*)sb.p;
+      double* sx = scal + step_offset(spec);
+      const void* xp[1] = {x->data};
+      multi_dot_dev(c, dt, n, 1, xp, x->data, sx);
+      axpby_devscalar(c, dt, n, sx, 0, x->data, V[0]->data);
+      lanczos_cycle_dev(c, m, V, spec, w, scal);
+      std::vector<double> hs(nscal);
+      NSG_CUDA(cudaMemcpyAsync(hs.data(), scal, sizeof(double) * nscal, cudaMemcpyDeviceToHost, c->stream));
+      NSG_CUDA(cudaStreamSynchronize(c->stream));
+      auto in_range = [](double q) { return std::isfinite(q) && q > 1e-280 && q < 1e280; };
+      const double qx = hs[step_offset(spec)];
+      if (qx == 0.0) break;
+      if (in_range(qx)) {
+        beta0 = std::sqrt(qx);
+        for (int j = 0; j < spec; ++j) {
+          const double* blk = hs.data() + step_offset(j);
+          const double a = blk[2 * j] + blk[2 * (j + 1) + 2 * j];
+          const double q = blk[4 * (j + 1)];
+          if (!std::isfinite(a) || !std::isfinite(q)) break;
+          const double b = std::sqrt(q);
+          alpha.push_back(a);
+          beta.push_back(b);
+          ++ops;
+          k = j + 1;
+          expm_col(k, remaining, E);
+          err = beta0 * b * std::abs(E[k - 1]);
+          if (err <= tol || b <= tol * 1e-3 || j + 1 == krylovdim) {
+            spec_ok = true;
+            break;
+          }
+          if (!in_range(q)) break;
+          if (j + 1 == spec) resume = spec;  // not converged yet: w holds step spec-1's vector
+        }
+      }
+    }
+    if (!spec_ok && resume > 0) {
+      // continue step by step: the next basis vector from w, as the step-by-step form does
+      axpby(c, dt, n, 1.0 / beta[resume - 1], 0.0, w->data, 0.0, 0.0, V[resume]->data);
+    } else if (!spec_ok) {
+      alpha.clear();
+      beta.clear();
+      ops = ops_before;
+      k = 0;
+      err = INFINITY;
+      beta0 = norm2(c, dt, n, x->data);
+      if (beta0 == 0.0) break;
+      NSG_CHECK(std::isfinite(beta0), NSG_ERR_NONFINITE, "exponentiate: non-finite vector");
+      axpby(c, dt, n, 1.0 / beta0, 0.0, x->data, 0.0, 0.0, V[0]->data);
+    }
+    for (int j = spec_ok ? krylovdim : resume; j < krylovdim; ++j) {
       double a, b;
       beta.resize(j + 1);
       lanczos_step(c, m, V, j, w, beta, &a, &b);
@@ -267,6 +413,7 @@ int nsg_exponentiate(nsg_ctx* c, nsg_linmap* m, double t_re, double t_im, nsg_te
       if (err <= tol || b <= tol * 1e-3 || j + 1 == krylovdim) break;
       axpby(c, dt, n, 1.0 / b, 0.0, w->data, 0.0, 0.0, V[j + 1]->data);
     }
+    c->krylov_hint = k;
     cd step = remaining;
     if (!(err <= tol || beta[k - 1] <= tol * 1e-3)) {
       // largest fraction of the remaining step within the per-unit-time error budget

@@ -54,6 +54,9 @@ struct nsg_ctx {
   int precision = NSG_PREC_FP64;
   std::string err;
   uint64_t launches = 0, flops = 0, contractions = 0, applies = 0;
+  // Krylov dimension the last exponentiate cycle used: the next cycle runs that many
+  // steps without host synchronisation before it checks convergence
+  int krylov_hint = 0;
   // pinned host staging for scalar readback
   double* host_scalars = nullptr;
   size_t host_scalars_cap = 0;
@@ -168,6 +171,13 @@ void multi_dot(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, c
 // w += sum_j coef_j v_j (coef complex pairs)
 void multi_axpy(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v,
                 const double* coef, void* w);
+// device-resident forms (no host synchronisation): the dot products land in out_dev
+// (2 doubles each); the coefficients / the sum of squares are read from device memory
+void multi_dot_dev(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, const void* w, double* out_dev);
+void multi_axpy_devcoef(nsg_ctx* c, int dtype, int64_t n, int nv, const void* const* v, const double* coef_dev,
+                        double sign, void* w);
+// y = x / sqrt(s) (mode 0) or y -= sqrt(s) x (mode 1), s = s_dev[0]
+void axpby_devscalar(nsg_ctx* c, int dtype, int64_t n, const double* s_dev, int mode, const void* x, void* y);
 double norm2(nsg_ctx* c, int dtype, int64_t n, const void* x);
 double amax(nsg_ctx* c, int dtype, int64_t n, const void* x);  // max |component|
 void scale(nsg_ctx* c, int dtype, int64_t n, double ar, double ai, void* x);

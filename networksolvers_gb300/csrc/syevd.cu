@@ -16,6 +16,8 @@
 // polls, raises an error flag and the host reports NSG_ERR_TIMEOUT.
 #include "nsg_internal.h"
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <cmath>
 #include <cstdlib>
@@ -422,6 +424,187 @@ __global__ void __launch_bounds__(NT)
       d[0] = cre(A[0]);
     }
   }
+}
+
+// Householder tridiagonalisation of a Hermitian matrix of moderate order (n <= ~640) by
+// one thread-block cluster: the matrix is held in the cluster's distributed shared
+// memory (column j in CTA j mod C, C <= 16), so a step's data never leaves the SMs and
+// its synchronisation is the hardware cluster barrier instead of a grid barrier over
+// global memory.  Same reflectors, tau, d and e as tridiag_kernel (the back-
+// transformation reads v_k below the subdiagonal of A's column k).
+// Step k: every CTA reads the pivot column from its owner (DSMEM), forms the reflector
+// (identically in every CTA: same data, same reduction order); each CTA forms
+// x_j = tau A22[:, j]^H v for its own columns; barrier; every CTA gathers x, forms
+// w = x - tau/2 (x^H v) v and applies A22 -= v w^H + w v^H to its own columns; barrier.
+constexpr int kClusterTriThreads = 256;
+
+template <typename T>
+__global__ void __launch_bounds__(kClusterTriThreads)
+    tridiag_cluster_kernel(T* __restrict__ A, int n, double* __restrict__ d, double* __restrict__ e,
+                           T* __restrict__ tau) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int C = int(cluster.num_blocks());
+  const int rank = int(cluster.block_rank());
+  const int ncol = (n - rank + C - 1) / C;  // columns j = rank + C q, q < ncol
+  const int ncmax = (n + C - 1) / C;        // the layout is the same in every CTA (remote
+                                            // reads address a peer's arrays by this offset)
+  extern __shared__ __align__(16) unsigned char ct_smem[];
+  T* cols = (T*)ct_smem;               // own columns, n rows each
+  T* vcur = cols + (size_t)ncmax * n;  // reflector (rows k+1..n-1 at offsets 0..m-1)
+  T* xloc = vcur + n;                  // x_j of own columns (by global column index)
+  T* xall = xloc + n;                  // gathered x (rows k+1.. at offsets 0..)
+  T* wv = xall + n;                    // w
+  __shared__ T red[kClusterTriThreads / 32];
+  __shared__ double redd[kClusterTriThreads / 32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  constexpr int NW = kClusterTriThreads / 32;
+  for (int q = 0; q < ncol; ++q) {
+    const T* src = A + (size_t)(rank + C * q) * n;
+    for (int r = tid; r < n; r += blockDim.x) cols[(size_t)q * n + r] = src[r];
+  }
+  cluster.sync();
+  auto bsum_d = [&](double v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (lane == 0) redd[warp] = v;
+    __syncthreads();
+    double s = 0.0;
+    for (int w = 0; w < NW; ++w) s += redd[w];
+    return s;
+  };
+  auto bsum_t = [&](T v) {
+    for (int o = 16; o > 0; o >>= 1) {
+      if constexpr (sizeof(T) == 8) {
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+      } else {
+        double2 t2;
+        t2.x = __shfl_xor_sync(0xffffffffu, ((double2&)v).x, o);
+        t2.y = __shfl_xor_sync(0xffffffffu, ((double2&)v).y, o);
+        v = cadd(v, *(T*)&t2);
+      }
+    }
+    __syncthreads();
+    if (lane == 0) red[warp] = v;
+    __syncthreads();
+    T s = czero<T>();
+    for (int w = 0; w < NW; ++w) s = cadd(s, red[w]);
+    return s;
+  };
+  for (int k = 0; k < n - 2; ++k) {
+    const int m = n - k - 1;
+    const int owner = k % C;
+    const T* pcol = cluster.map_shared_rank(cols, owner) + (size_t)(k / C) * n;
+    // 1. the reflector from column k (rows k+1..n-1), in every CTA
+    double ss = 0.0;
+    for (int r = tid; r < m; r += blockDim.x) {
+      const T a = pcol[k + 1 + r];
+      vcur[r] = a;
+      if (r > 0) ss += cabs2(a);
+    }
+    T dk = czero<T>();
+    if (rank == owner && tid == 0) dk = pcol[k];
+    const double xnorm2 = bsum_d(ss);  // its barriers publish vcur
+    const T alpha = vcur[0];
+    const double ar = cre(alpha);
+    double ai = 0.0;
+    if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
+    T tk = czero<T>();
+    double beta = ar;
+    T scl = czero<T>();
+    const bool active = !(xnorm2 == 0.0 && ai == 0.0);
+    if (active) {
+      const double nrm = sqrt(ar * ar + ai * ai + xnorm2);
+      beta = ar >= 0 ? -nrm : nrm;
+      if constexpr (sizeof(T) == 16) {
+        double2 t2 = make_double2((beta - ar) / beta, -ai / beta);
+        tk = *(T*)&t2;
+        double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
+        scl = *(T*)&inv;
+      } else {
+        double t1 = (beta - ar) / beta, s1 = 1.0 / (ar - beta);
+        tk = *(T*)&t1;
+        scl = *(T*)&s1;
+      }
+    }
+    __syncthreads();  // every thread has read vcur[0]
+    for (int r = tid; r < m; r += blockDim.x) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scl);
+    __syncthreads();
+    if (rank == owner) {
+      if (tid == 0) {
+        d[k] = cre(dk);
+        e[k] = active ? beta : ar;
+        tau[k] = tk;
+      }
+      T* gcol = A + (size_t)k * n + (k + 1);
+      for (int r = tid + 1; r < m; r += blockDim.x) gcol[r] = vcur[r];
+    }
+    // 2. x_j = tau sum_i conj(A_ij) v_i for the own trailing columns (one warp per column)
+    const int q0 = (k + 1 - rank + C - 1) / C;  // first own column index with j >= k+1
+    if (active) {
+      for (int q = q0 + warp; q < ncol; q += NW) {
+        const int j = rank + C * q;
+        const T* cj = cols + (size_t)q * n + (k + 1);
+        T acc = czero<T>(), acc1 = czero<T>();
+        int r = lane;
+        for (; r + 32 < m; r += 64) {
+          acc = fcma(acc, cj[r], vcur[r]);
+          acc1 = fcma(acc1, cj[r + 32], vcur[r + 32]);
+        }
+        if (r < m) acc = fcma(acc, cj[r], vcur[r]);
+        acc = cadd(acc, acc1);
+        for (int o = 16; o > 0; o >>= 1) {
+          if constexpr (sizeof(T) == 8) {
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+          } else {
+            double2 t2;
+            t2.x = __shfl_xor_sync(0xffffffffu, ((double2&)acc).x, o);
+            t2.y = __shfl_xor_sync(0xffffffffu, ((double2&)acc).y, o);
+            acc = cadd(acc, *(T*)&t2);
+          }
+        }
+        if (lane == 0) xloc[j] = cmulv(tk, acc);
+      }
+    }
+    cluster.sync();
+    if (active) {
+      // 3. gather x, x^H v, w = x - tau/2 (x^H v) v
+      T pv = czero<T>();
+      for (int r = tid; r < m; r += blockDim.x) {
+        const int j = k + 1 + r;
+        const T xj = cluster.map_shared_rank(xloc, j % C)[j];
+        xall[r] = xj;
+        pv = cadd(pv, cmulv(cconj(xj), vcur[r]));
+      }
+      const T xv = bsum_t(pv);
+      const T alpha2 = cscale(cmulv(tk, xv), -0.5);
+      for (int r = tid; r < m; r += blockDim.x) wv[r] = cadd(xall[r], cmulv(alpha2, vcur[r]));
+      __syncthreads();
+      // 4. A22 -= v w^H + w v^H on the own trailing columns
+      for (int q = q0 + warp; q < ncol; q += NW) {
+        const int jr = rank + C * q - (k + 1);
+        T* cj = cols + (size_t)q * n + (k + 1);
+        const T wj = cconj(wv[jr]), vj = cconj(vcur[jr]);
+        for (int r = lane; r < m; r += 32) cj[r] = fnms2(cj[r], vcur[r], wj, wv[r], vj);
+      }
+    }
+    cluster.sync();
+  }
+  // the last 2 x 2 block
+  if (n >= 2) {
+    const int o2 = (n - 2) % C, o1 = (n - 1) % C;
+    if (rank == o2 && tid == 0) {
+      const T* c2 = cols + (size_t)((n - 2) / C) * n;
+      const T a11 = c2[n - 2], a21 = c2[n - 1];
+      d[n - 2] = cre(a11);
+      e[n - 2] = cre(a21);
+      A[(n - 1) + (size_t)(n - 2) * n] = a21;
+    }
+    if (rank == o1 && tid == 0) d[n - 1] = cre(cols[(size_t)((n - 1) / C) * n + (n - 1)]);
+  } else if (rank == 0 && tid == 0) {
+    d[0] = cre(cols[0]);
+  }
+  cluster.sync();  // no CTA leaves while another may still read its shared memory
 }
 
 // For complex A the last subdiagonal element may be complex: handled on the host by a
@@ -1362,6 +1545,53 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
   check_launch("back_transform");
 }
 
+// Cluster tridiagonalisation when the matrix fits the distributed shared memory of one
+// cluster (up to 16 CTAs of ~200 KB): cluster size 2..16 by order (more SMs for more
+// FP64 work, fewer for fewer remote reads), raised until the columns fit.  Returns false
+// (nothing launched) when no cluster shape fits; the caller then takes the grid kernel.
+// NSG_TRI_CLUSTER_MAX (default 640) caps the order routed here.
+template <typename T>
+static bool tridiag_cluster(nsg_ctx* c, int n, T* A, double* d, double* e, T* tau) {
+  static int cap = [] {
+    const char* s = std::getenv("NSG_TRI_CLUSTER_MAX");
+    return s ? std::atoi(s) : 640;
+  }();
+  if (n > cap || n < 3) return false;
+  const size_t eb = sizeof(T);
+  int C = n <= 64 ? 2 : n <= 128 ? 4 : n <= 256 ? 8 : 16;
+  auto kfn = tridiag_cluster_kernel<T>;
+  for (; C <= 16; C *= 2) {
+    const size_t ncol = (size_t(n) + C - 1) / C;
+    const size_t smem = (ncol * n + 4 * size_t(n)) * eb;
+    if (smem > 200 * 1024) continue;
+    ensure_smem_limit((const void*)kfn, int(smem));
+    if (C > 8) NSG_CUDA(cudaFuncSetAttribute((const void*)kfn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kClusterTriThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = c->stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)kfn, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    ProfScope ps(c, NSG_PROF_TRIDIAG, (sizeof(T) == 16 ? 16.0 : 4.0) / 3.0 * double(n) * n * n);
+    NSG_CUDA(cudaLaunchKernelEx(&cfg, kfn, A, n, d, e, tau));
+    count_launch(c);
+    check_launch("tridiag (cluster)");
+    return true;
+  }
+  return false;
+}
+
 // Hermitian eigen-decomposition of A (n x n, consumed).  Eigenvalues ascending into
 // w_host; eigenvectors for the eigenvalue indices `cols` (ascending order indices)
 // into Zout (n x ncols, column-major).  The caller chooses cols after seeing the
@@ -1377,6 +1607,10 @@ static void syevd_dc_impl(nsg_ctx* c, int dtype, int n, T* A, std::vector<double
     NSG_CUDA(cudaMemcpyAsync(&a, A, eb, cudaMemcpyDeviceToHost, c->stream));
     NSG_CUDA(cudaStreamSynchronize(c->stream));
     d[0] = ((double*)&a)[0];
+  } else if (tridiag_cluster<T>(c, n, A, dd.as<double>(), de.as<double>(), dtau.as<T>())) {
+    NSG_CUDA(cudaMemcpyAsync(d.data(), dd.p, sizeof(double) * n, cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaMemcpyAsync(e.data(), de.p, sizeof(double) * (n - 1), cudaMemcpyDeviceToHost, c->stream));
+    NSG_CUDA(cudaStreamSynchronize(c->stream));
   } else {
     // cooperative tridiagonalisation
     int max_blocks = 0;

@@ -45,15 +45,21 @@ def _matricize(T: Tensor, left):
     return M.reshape(ml, -1), left, right
 
 
-def factorize(T: Tensor, left, cutoff=0.0, maxdim=None, mindim=1, tags="Link"):
+def factorize(T: Tensor, left, cutoff=0.0, maxdim=None, mindim=1, tags="Link", return_gap=False):
     """U·C = T truncated; U an isometry on `left` (ortho="left"), C = S·V†.
-    Returns (U, C, truncerr, spectrum_kept)."""
+    Returns (U, C, truncerr, spectrum_kept), and with return_gap the relative gap of the
+    cut, (s_k^2 - s_{k+1}^2) / s_k^2 between the last kept and the first discarded weight
+    (inf when nothing is discarded): near zero, the cut runs through a (near-)degenerate
+    multiplet and the kept subspace is fixed only up to rotations inside it."""
     M, L, R = _matricize(T, left)
     u, s, vh = np.linalg.svd(M, full_matrices=False)
     n, err = truncate_spectrum(s * s, cutoff, maxdim, mindim)
     link = Index(n, tags)
     U = Tensor(u[:, :n].reshape([i.dim for i in L] + [n]), L + [link])
     C = Tensor((s[:n, None] * vh[:n]).reshape([n] + [i.dim for i in R]), [link] + R)
+    if return_gap:
+        gap = float("inf") if n >= len(s) or s[n - 1] == 0 else float((s[n - 1] ** 2 - s[n] ** 2) / s[n - 1] ** 2)
+        return U, C, err, s[:n] ** 2, gap
     return U, C, err, s[:n] ** 2
 
 

@@ -198,9 +198,9 @@ def inserter(problem, local, R, sweep, normalize=False, set_orthogonal_region=Tr
     if len(region) == 1:
         C = local
     elif len(region) == 2:
-        U, C, err, spec = linalg.factorize(local, list(psi[region[0]].inds), **trunc)
+        U, C, err, spec, gap = linalg.factorize(local, list(psi[region[0]].inds), return_gap=True, **trunc)
         psi[region[0]] = U
-        info = dict(truncerr=err, newdim=U.inds[-1].dim)
+        info = dict(truncerr=err, newdim=U.inds[-1].dim, cut_gap=gap)
     else:
         raise ValueError(f"Region of length {len(region)} not currently supported")
     v = region[-1]

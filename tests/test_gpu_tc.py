@@ -96,3 +96,37 @@ def test_ozaki8_gemm_fp64_accuracy(nsg_ctx, m, k, n):
     scale = np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :] * k
     assert np.max(np.abs(c - ref) / scale) < 1e-15
     assert rel(c, ref) < 1e-13
+
+
+@pytest.mark.parametrize("precision,bound", [("ozaki", 1e-13), ("ozaki8", 1e-15)])
+def test_complex_ozaki_gemm(nsg_ctx, precision, bound):
+    """The split form for complex tensors: four real slice products on the interleaved
+    real and imaginary parts (Re C = Ar Br - sa sb Ai Bi, Im C = sb Ar Bi + sa Ai Br, the
+    signs from conjugated operands), in every operand orientation and with conjugation;
+    within the real products' bound relative to the row and column scales, and on the
+    tensor cores (the tcgen05 class launches)."""
+    rng = np.random.default_rng(11)
+    m, k, n = 200, 130, 96
+    i, j, l = Index(m), Index(n), Index(k)
+    a = rng.standard_normal((m, k)) + 1j * rng.standard_normal((m, k))
+    b = rng.standard_normal((k, n)) + 1j * rng.standard_normal((k, n))
+    a[:, 0] *= 1e3
+    scale = np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :] * k
+    cases = [(((i, l), a), ((l, j), b), False, False), (((l, i), a.T.copy()), ((l, j), b), False, False),
+             (((i, l), a), ((j, l), b.T.copy()), False, False), (((i, l), a), ((l, j), b), True, False),
+             (((l, i), a.T.copy()), ((j, l), b.T.copy()), True, True)]
+    for (ia, aa), (ib, bb), ca, cb in cases:
+        A, B = DTensor.from_numpy(aa, ia), DTensor.from_numpy(bb, ib)
+        A = A.dag() if ca else A
+        B = B.dag() if cb else B
+        ref = (np.conj(a) if ca else a) @ (np.conj(b) if cb else b)
+        nsg_ctx.set_precision(precision)
+        nsg_ctx.profile(True)
+        try:
+            c = contract([A, B], out=[i, j]).to_numpy()
+            prof = nsg_ctx.profile_read()
+        finally:
+            nsg_ctx.profile(False)
+            nsg_ctx.set_precision("fp64")
+        assert prof["tc_gemm"]["launches"] == 4, prof
+        assert np.max(np.abs(c - ref) / scale) < bound, (ia, ib, ca, cb)
