@@ -1549,12 +1549,14 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
 // cluster (up to 16 CTAs of ~200 KB): cluster size 2..16 by order (more SMs for more
 // FP64 work, fewer for fewer remote reads), raised until the columns fit.  Returns false
 // (nothing launched) when no cluster shape fits; the caller then takes the grid kernel.
-// NSG_TRI_CLUSTER_MAX (default 640) caps the order routed here.
+// NSG_TRI_CLUSTER_MAX (default 360) caps the order routed here: measured on GB300 the
+// cluster kernel is 1.7x / 1.45x / 1.17x faster than the grid kernel at orders 64 / 128 /
+// 256 and 3 % slower at 475.
 template <typename T>
 static bool tridiag_cluster(nsg_ctx* c, int n, T* A, double* d, double* e, T* tau) {
   static int cap = [] {
     const char* s = std::getenv("NSG_TRI_CLUSTER_MAX");
-    return s ? std::atoi(s) : 640;
+    return s ? std::atoi(s) : 360;
   }();
   if (n > cap || n < 3) return false;
   const size_t eb = sizeof(T);
