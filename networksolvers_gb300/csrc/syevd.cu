@@ -1547,7 +1547,7 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
 
 // Cluster tridiagonalisation when the matrix fits the distributed shared memory of one
 // cluster (up to 16 CTAs of ~200 KB): cluster size 2..16 by order (more SMs for more
-// FP64 work, fewer for fewer remote reads), raised until the columns fit.  Returns false
+// FP64 work), raised until the columns fit.  Returns false
 // (nothing launched) when no cluster shape fits; the caller then takes the grid kernel.
 // NSG_TRI_CLUSTER_MAX (default 360) caps the order routed here: measured on GB300 the
 // cluster kernel is 1.7x / 1.45x / 1.17x faster than the grid kernel at orders 64 / 128 /
@@ -1560,7 +1560,9 @@ static bool tridiag_cluster(nsg_ctx* c, int n, T* A, double* d, double* e, T* ta
   }();
   if (n > cap || n < 3) return false;
   const size_t eb = sizeof(T);
-  int C = n <= 64 ? 2 : n <= 128 ? 4 : n <= 256 ? 8 : 16;
+  // the reduction is FP64-bound on its C SMs (ncu at n = 256, C = 8: FP64 pipe 70 % of
+  // the active SMs' peak), and a CTA's remote reads per step do not grow with C
+  int C = n <= 32 ? 2 : n <= 64 ? 4 : n <= 128 ? 8 : 16;
   auto kfn = tridiag_cluster_kernel<T>;
   for (; C <= 16; C *= 2) {
     const size_t ncol = (size_t(n) + C - 1) / C;

@@ -5,16 +5,17 @@
   expansion, Lanczos krylovdim 3 / maxiter 1) over its first three sweeps (maxdim 64,
   128, 256), region by region, in the plain FP64 form and in the split-precision form:
   energies within 1e-10 relative and truncated bond dimensions exactly equal over the
-  first two sweeps, and over the third up to the first region whose truncation is not
-  fixed by FP64 arithmetic (a cutoff tie: the discarded weight of one of the two
-  decisions within 1e-14 of the cutoff, relative to the total weight); the energies
-  after the three sweeps within 1e-7.  Inside the third sweep the two runs drift apart
-  before any count differs: at maxdim 256 the truncation cuts through spectra whose
-  multiplets (the Heisenberg chain's SU(2) symmetry) are split only by the state's
-  residual asymmetry, so rounding-level differences rotate the kept subspace and grow
-  from region to region.  The same drift appears between two plain FP64 GPU runs whose
-  starts differ by 1e-13 (4e-9 after sweep 3, 7e-10 after the 10-sweep run), so it is
-  the configuration's sensitivity, not an arithmetic error of either side.
+  first sweep; over sweeps 2-3 energies within 1e-7 region by region up to the first
+  differing count, which must be a cutoff tie (the discarded weight of one of the two
+  decisions within 1e-14 of the cutoff, relative to the total weight) or follow the
+  drift; the energies after the three sweeps within 1e-7.  From sweep 2 on the runs
+  drift apart before any count differs: the truncations (of the factorization and of
+  the expansion's eigen(rho)) cut through spectra whose multiplets (the Heisenberg
+  chain's SU(2) symmetry) are split only by the state's residual asymmetry, so
+  rounding-level differences rotate the kept subspaces and grow from region to region.
+  Two plain FP64 GPU runs whose starts differ by 1e-13 drift the same way (4e-9 after
+  sweep 3, 7e-10 after the 10-sweep run): the configuration's sensitivity, not an
+  arithmetic error of either side.
 * 2-site TDVP on the depth-5 binary-tree TFIM (63 sites, h = 1, all-up start, dt = 0.05,
   maxdim 256, cutoff 1e-9, Krylov exponential tol 1e-12) over two time steps: fidelity
   with the oracle's state >= 1 - 1e-8 and equal bond dimensions.
@@ -62,17 +63,17 @@ def test_c3_first_three_sweeps_match_oracle(nsg_ctx, c3_oracle, precision):
         nsg_ctx.set_precision("fp64")
     assert r.shape == ro.shape
     cutoff = 1e-12
-    per_sweep = 2 * (100 - 1)
-    strict = 2 * per_sweep  # sweeps 1 and 2, region by region
+    strict = 2 * (100 - 1)  # sweep 1, region by region
     diff = np.nonzero(r[:, 3] != ro[:, 3])[0]
     first_diff = int(diff[0]) if len(diff) else len(r)
     assert first_diff >= strict, (first_diff, r[first_diff], ro[first_diff])
-    rel = np.abs(r[:strict, 2] - ro[:strict, 2]) / np.abs(ro[:strict, 2])
-    assert np.max(rel) < 1e-10, (np.argmax(rel), np.max(rel))
+    rel = np.abs(r[:, 2] - ro[:, 2]) / np.abs(ro[:, 2])
+    assert np.max(rel[:strict]) < 1e-10, (np.argmax(rel[:strict]), np.max(rel[:strict]))
+    assert np.max(rel[:first_diff]) < 1e-7, (np.argmax(rel[:first_diff]), np.max(rel[:first_diff]))
     if first_diff < len(r):
-        # the first differing count in sweep 3 is a cutoff tie or follows the drift
+        # the first differing count is a cutoff tie or follows the drift
         margin = min(abs(ro[first_diff, 4] - cutoff), abs(r[first_diff, 4] - cutoff))
-        drift = np.max(np.abs(r[strict:first_diff, 2] - ro[strict:first_diff, 2]) / np.abs(ro[strict:first_diff, 2]))
+        drift = np.max(rel[strict:first_diff])
         assert margin < 1e-14 or drift > 1e-10, (first_diff, margin, drift)
         assert abs(int(r[first_diff, 3]) - int(ro[first_diff, 3])) <= 2
     assert abs(E - Eo) / abs(Eo) < 1e-7
