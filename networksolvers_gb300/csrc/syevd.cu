@@ -319,18 +319,22 @@ __global__ void __launch_bounds__(NT)
     target += unsigned(nact);
     __syncthreads();
     if (tid == 0) {
-      __threadfence();
-      atomicAdd(&bar->count, 1u);
-      volatile unsigned int* vcount = &bar->count;
+      // arrival with release semantics (the block barrier above orders every thread's
+      // stores of this step before it), polling with acquire semantics (the peers' stores
+      // are visible after it, and the block barrier below passes that on): the same
+      // ordering as full fences on both sides, without their cost
+      asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(&bar->count), "r"(1u) : "memory");
       long long polls = 0;
-      while (int(*vcount - target) < 0) {
+      for (;;) {
+        unsigned int cnt;
+        asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(cnt) : "l"(&bar->count) : "memory");
+        if (int(cnt - target) >= 0) break;
         if (++polls > (1ll << 26) || *(volatile int*)&bar->err) {
           atomicExch(&bar->err, 1);
           break;
         }
         __nanosleep(20);
       }
-      __threadfence();
       s_ok = (*(volatile int*)&bar->err) == 0;
     }
     __syncthreads();
@@ -892,18 +896,27 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
       W.kind[lo + t] = kd[t];
     }
   }
-  // the deflation rotations, in order, on the block's columns of Q (one row per thread)
-  const int nrot = s_nrot;
-  if (nrot > 0) {
-    for (int r = threadIdx.x; r < nb; r += blockDim.x) {
-      double* row = Q + (lo + r);
-      for (int q = 0; q < nrot; ++q) {
-        const size_t cp = (size_t)(lo + rpq[2 * q]) * n, ci = (size_t)(lo + rpq[2 * q + 1]) * n;
-        const double c = rcs[2 * q], sn = rcs[2 * q + 1];
-        const double xp = row[cp], xi = row[ci];
-        row[cp] = c * xp - sn * xi;
-        row[ci] = sn * xp + c * xi;
-      }
+  (void)s_nrot;
+}
+
+// The deflation rotations of every merge of a level, in order, on the block's columns of
+// Q: one thread per row (blockIdx.y = merge), so a merge's rows are spread over many SMs
+// and each thread's chain of dependent rotations is one row long.
+__global__ void dc_rotate_kernel(double* __restrict__ Q, int n, const MergeDesc* __restrict__ md, DcWork W) {
+  const int mi = blockIdx.y;
+  const int nrot = W.counts[3 * mi + 1];
+  if (nrot == 0) return;
+  const int lo = md[mi].lo, nb = md[mi].hi - lo;
+  const int* rpq = W.rot_pq + 2 * lo;
+  const double* rcs = W.rot_cs + 2 * lo;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nb; r += gridDim.x * blockDim.x) {
+    double* row = Q + (lo + r);
+    for (int q = 0; q < nrot; ++q) {
+      const size_t cp = (size_t)(lo + rpq[2 * q]) * n, ci = (size_t)(lo + rpq[2 * q + 1]) * n;
+      const double c = rcs[2 * q], sn = rcs[2 * q + 1];
+      const double xp = row[cp], xi = row[ci];
+      row[cp] = c * xp - sn * xi;
+      row[ci] = sn * xp + c * xi;
     }
   }
 }
@@ -1382,8 +1395,9 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       if (shm) raise_smem_limit((const void*)dc_prep_kernel, shm);
       ProfScope ps(c, NSG_PROF_DC, 0.0);
       dc_prep_kernel<<<nm, 256, shm, c->stream>>>(w, Q, n, md, W);
+      dc_rotate_kernel<<<dim3((nbmax + 127) / 128, nm), 128, 0, c->stream>>>(Q, n, md, W);
     }
-    count_launch(c);
+    count_launch(c, 2);
     check_launch("dc prep");
     NSG_CUDA(cudaMemcpyAsync(cnt.data(), W.counts, sizeof(int) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
     int leaf_failed = 0;
