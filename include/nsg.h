@@ -110,6 +110,15 @@ int nsg_ctx_profile_read(nsg_ctx* ctx, int cls, uint64_t* launches, double* ms, 
  * that status into an error. */
 int nsg_ctx_wait_probe(nsg_ctx* ctx, int64_t polls);
 
+/* Launch-choice override of this context, for the autotuner that writes the library's
+ * compiled-in tuning table (no counterpart in the reference).  param NSG_TUNE_SPLITK:
+ * number of K slices of the FP64 CUDA-core GEMM (1..64; 0 restores the table);
+ * NSG_TUNE_TRIDIAG: the Householder tridiagonalisation's path (-1 the grid-wide kernel,
+ * 2/4/8/16 one thread-block cluster of that size where the matrix fits it, 0 the table). */
+#define NSG_TUNE_SPLITK 0
+#define NSG_TUNE_TRIDIAG 1
+int nsg_ctx_set_tuning(nsg_ctx* ctx, int param, int value);
+
 /* ---- tensors ------------------------------------------------------------- */
 int nsg_tensor_create(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims, nsg_tensor** out);
 int nsg_tensor_upload(nsg_ctx* ctx, int dtype, int rank, const int64_t* dims,

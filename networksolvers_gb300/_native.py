@@ -52,6 +52,7 @@ _SIGS = {
     "nsg_ctx_profile": (i32, [p, i32]),
     "nsg_ctx_profile_read": (i32, [p, i32, C.POINTER(u64), P_dbl, P_dbl]),
     "nsg_ctx_wait_probe": (i32, [p, i64]),
+    "nsg_ctx_set_tuning": (i32, [p, i32, i32]),
     "nsg_tensor_create": (i32, [p, i32, i32, P_i64, P_p]),
     "nsg_tensor_upload": (i32, [p, i32, i32, P_i64, p, P_p]),
     "nsg_tensor_download": (i32, [p, p, p]),
@@ -150,6 +151,12 @@ class Context:
         f = C.c_float()
         self.check(self.L.nsg_ctx_event_elapsed(self.h, a, b, C.byref(f)))
         return f.value
+
+    def set_tuning(self, param, value):
+        """Launch-choice override (0 restores the compiled-in tuning table): param
+        "splitk" (FP64 GEMM K slices, 1..64) or "tridiag" (-1 grid kernel, 2..16 cluster)."""
+        code = {"splitk": 0, "tridiag": 1}[param]
+        self.check(self.L.nsg_ctx_set_tuning(self.h, code, int(value)))
 
     def profile(self, enable):
         self.check(self.L.nsg_ctx_profile(self.h, int(enable)))

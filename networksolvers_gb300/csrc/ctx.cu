@@ -150,6 +150,22 @@ using namespace nsg;
 
 extern "C" {
 
+int nsg_ctx_set_tuning(nsg_ctx* c, int param, int value) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c, NSG_ERR_INVALID, "null context");
+  if (param == NSG_TUNE_SPLITK) {
+    NSG_CHECK(value >= 0 && value <= 64, NSG_ERR_INVALID, "tuning: split-K count 0..64");
+    c->tune_splitk = value;
+  } else if (param == NSG_TUNE_TRIDIAG) {
+    NSG_CHECK(value == 0 || value == -1 || value == 2 || value == 4 || value == 8 || value == 16, NSG_ERR_INVALID,
+              "tuning: tridiagonalisation path -1, 0, 2, 4, 8 or 16");
+    c->tune_tri = value;
+  } else {
+    NSG_CHECK(false, NSG_ERR_INVALID, "tuning: unknown parameter");
+  }
+  NSG_API_END(c)
+}
+
 int nsg_ctx_wait_probe(nsg_ctx* c, int64_t polls) {
   NSG_API_BEGIN(c)
   NSG_CHECK(c, NSG_ERR_INVALID, "null context");

@@ -6,6 +6,7 @@
 // thread keeps the FP64 pipes busy.  Loads are mapped so that consecutive threads
 // touch consecutive addresses for either operand orientation.
 #include "nsg_internal.h"
+#include "tuning_table.h"
 
 #include <algorithm>
 #include <map>
@@ -282,6 +283,20 @@ void gemm_f64_simt(nsg_ctx* c, const GemmArgs& g) {
     int64_t maxs = g.K >= 512 ? g.K / 256 : g.K / 32;
     splits = int(std::min<int64_t>({want, maxs, 64}));
     if (splits < 2) splits = 1;
+    ksplit = (g.K + splits - 1) / splits;
+    ksplit = ((ksplit + 15) / 16) * 16;
+    splits = int((g.K + ksplit - 1) / ksplit);
+  }
+  // the tuning table (or the context's override) replaces the rule for its buckets
+  int tuned = c->tune_splitk;
+  if (tuned == 0)
+    for (const auto& t : tuning::kSplit)
+      if (t.splits > 0 && tiles <= t.max_tiles && g.K <= t.max_k) {
+        tuned = t.splits;
+        break;
+      }
+  if (tuned > 0) {
+    splits = int(std::min<int64_t>(tuned, std::max<int64_t>(1, g.K / 16)));
     ksplit = (g.K + splits - 1) / splits;
     ksplit = ((ksplit + 15) / 16) * 16;
     splits = int((g.K + ksplit - 1) / ksplit);

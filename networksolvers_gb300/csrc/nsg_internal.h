@@ -57,6 +57,9 @@ struct nsg_ctx {
   // Krylov dimension the last exponentiate cycle used: the next cycle runs that many
   // steps without host synchronisation before it checks convergence
   int krylov_hint = 0;
+  // launch-choice overrides set by nsg_ctx_set_tuning (0: the compiled-in tuning table)
+  int tune_splitk = 0;  // FP64 GEMM K slices (> 0 forces that count)
+  int tune_tri = 0;     // tridiagonalisation: -1 grid kernel, 2..16 cluster size
   // pinned host staging for scalar readback
   double* host_scalars = nullptr;
   size_t host_scalars_cap = 0;

@@ -15,6 +15,7 @@
 // Every wait in these kernels is bounded: the grid barrier gives up after ~2^26
 // polls, raises an error flag and the host reports NSG_ERR_TIMEOUT.
 #include "nsg_internal.h"
+#include "tuning_table.h"
 
 #include <cooperative_groups.h>
 
@@ -1560,23 +1561,24 @@ static void back_transform(nsg_ctx* c, int dtype, int n, const T* A, const T* ta
 }
 
 // Cluster tridiagonalisation when the matrix fits the distributed shared memory of one
-// cluster (up to 16 CTAs of ~200 KB): cluster size 2..16 by order (more SMs for more
-// FP64 work), raised until the columns fit.  Returns false
-// (nothing launched) when no cluster shape fits; the caller then takes the grid kernel.
-// NSG_TRI_CLUSTER_MAX (default 360) caps the order routed here: measured on GB300 the
-// cluster kernel is 1.7x / 1.45x / 1.17x faster than the grid kernel at orders 64 / 128 /
-// 256 and 3 % slower at 475.
+// cluster (up to 16 CTAs of ~200 KB).  The cluster size comes from the tuning table by
+// order (measured: the reduction is FP64-bound on its C SMs, and a CTA's remote reads
+// per step do not grow with C; orders above the table take the grid kernel), or from the
+// context's override; it is raised until the columns fit.  Returns false (nothing
+// launched) for the grid kernel or when no cluster shape fits.
 template <typename T>
 static bool tridiag_cluster(nsg_ctx* c, int n, T* A, double* d, double* e, T* tau) {
-  static int cap = [] {
-    const char* s = std::getenv("NSG_TRI_CLUSTER_MAX");
-    return s ? std::atoi(s) : 360;
-  }();
-  if (n > cap || n < 3) return false;
+  if (n < 3 || c->tune_tri == -1) return false;
   const size_t eb = sizeof(T);
-  // the reduction is FP64-bound on its C SMs (ncu at n = 256, C = 8: FP64 pipe 70 % of
-  // the active SMs' peak), and a CTA's remote reads per step do not grow with C
-  int C = n <= 32 ? 2 : n <= 64 ? 4 : n <= 128 ? 8 : 16;
+  int C = c->tune_tri;
+  if (C == 0) {
+    for (const auto& t : tuning::kTri)
+      if (n <= t.max_order) {
+        C = t.path;
+        break;
+      }
+    if (C == 0) return false;
+  }
   auto kfn = tridiag_cluster_kernel<T>;
   for (; C <= 16; C *= 2) {
     const size_t ncol = (size_t(n) + C - 1) / C;
