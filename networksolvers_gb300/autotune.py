@@ -112,8 +112,19 @@ def tri_entries(rows):
 
 
 def split_entries(rows):
-    """(max_tiles, max_k, splits) entries in increasing (tiles, k): first match wins."""
-    return [(r["tiles"], r["k"], r["best"]) for r in sorted(rows, key=lambda r: (r["tiles"], r["k"]))]
+    """(max_tiles, max_k, splits) entries in increasing (tiles, k): first match wins.
+    Output sizes that fall in the same tile count (32 and 64 both make one 64 x 64 tile)
+    share a bucket, whose split count is the one with the least summed time over them."""
+    groups = {}
+    for r in rows:
+        groups.setdefault((r["tiles"], r["k"]), []).append(r["ms"])
+    out = []
+    for key in sorted(groups):
+        ms = groups[key]
+        common = set(ms[0]).intersection(*ms[1:])
+        best = min(common, key=lambda s: sum(t[s] for t in ms))
+        out.append((key[0], key[1], int(best)))
+    return out
 
 
 def header(tri, split, device_name):
@@ -159,7 +170,12 @@ def main(argv=None):
     ap = argparse.ArgumentParser(prog="python -m networksolvers_gb300.autotune")
     ap.add_argument("--out", default=str(Path(__file__).resolve().parent))
     ap.add_argument("--reps", type=int, default=5)
+    ap.add_argument("--from-json", default=None,
+                    help="rewrite the tables from a tuning.json of an earlier run, measuring nothing")
     args = ap.parse_args(argv)
+    if args.from_json:
+        d = json.loads(Path(args.from_json).read_text())
+        return _write(Path(args.out), d["device"], d["tridiag"], d["splitk"])
     from . import _native
     from .build import build
     build()
@@ -173,8 +189,11 @@ def main(argv=None):
         dev = "unknown GPU"
     tri_rows = tune_tridiag(ctx, args.reps)
     split_rows = tune_splitk(ctx, args.reps)
+    return _write(Path(args.out), dev, tri_rows, split_rows)
+
+
+def _write(out, dev, tri_rows, split_rows):
     tri, split = tri_entries(tri_rows), split_entries(split_rows)
-    out = Path(args.out)
     out.mkdir(parents=True, exist_ok=True)
     (out / "tuning.json").write_text(json.dumps({"device": dev, "tridiag": tri_rows, "splitk": split_rows,
                                                  "table": {"tridiag": tri, "splitk": split}}, indent=1) + "\n")

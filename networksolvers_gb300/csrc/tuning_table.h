@@ -2,6 +2,7 @@
 // (python -m networksolvers_gb300.autotune, which measures every candidate on the GPU and
 // writes this file and networksolvers_gb300/tuning.json).  Compiled in; a context can
 // override an entry for measurement (nsg_ctx_set_tuning).
+// Measured on: NVIDIA GB300.
 #pragma once
 
 namespace nsg {
@@ -15,7 +16,7 @@ struct TriEntry {
   int path;
 };
 constexpr TriEntry kTri[] = {
-    {32, 2}, {64, 4}, {128, 8}, {360, 16},
+    {32, 8}, {384, 16},
 };
 
 // FP64 CUDA-core GEMM: number of K slices (split K) for products whose output has
@@ -27,7 +28,27 @@ struct SplitEntry {
   int splits;
 };
 constexpr SplitEntry kSplit[] = {
-    {0, 0, 0},
+    {1, 64, 4},
+    {1, 128, 8},
+    {1, 256, 16},
+    {1, 512, 32},
+    {1, 1024, 64},
+    {1, 2048, 64},
+    {1, 4096, 64},
+    {4, 64, 4},
+    {4, 128, 8},
+    {4, 256, 16},
+    {4, 512, 32},
+    {4, 1024, 32},
+    {4, 2048, 32},
+    {4, 4096, 32},
+    {16, 64, 4},
+    {16, 128, 8},
+    {16, 256, 16},
+    {16, 512, 16},
+    {16, 1024, 64},
+    {16, 2048, 64},
+    {16, 4096, 64},
 };
 
 }  // namespace tuning

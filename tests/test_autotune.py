@@ -24,9 +24,13 @@ def test_entries_and_header_round_trip():
             {"order": 128, "best": 8}, {"order": 192, "best": -1}, {"order": 256, "best": 16}]
     tri = at.tri_entries(rows)
     assert tri == [(32, 2), (96, 4), (128, 8)]  # merged, and cut at the first grid-kernel order
-    srows = [{"tiles": 4, "k": 128, "best": 2}, {"tiles": 1, "k": 64, "best": 1}, {"tiles": 1, "k": 4096, "best": 32}]
+    srows = [{"tiles": 4, "k": 128, "ms": {"1": 2.0, "2": 1.0}},
+             {"tiles": 1, "k": 64, "ms": {"1": 1.0, "2": 1.5}},
+             {"tiles": 1, "k": 4096, "ms": {"16": 0.5, "32": 0.4}},
+             # a second output size with the same tile count: the summed time decides
+             {"tiles": 1, "k": 4096, "ms": {"16": 0.5, "32": 0.7}}]
     split = at.split_entries(srows)
-    assert split == [(1, 64, 1), (1, 4096, 32), (4, 128, 2)]
+    assert split == [(1, 64, 1), (1, 4096, 16), (4, 128, 2)]
     assert parse_header(at.header(tri, split, "test")) == (tri, split)
 
 
