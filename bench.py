@@ -635,8 +635,10 @@ def run_batch(args):
     t0 = time.perf_counter()
     seq = batch.SolvePool(workers=1, precision="fp64").run(jobs[:args.sample])
     t_seq = time.perf_counter() - t0
+    tuning = {"tridiag": args.pool_tridiag} if args.pool_tridiag else None
+    pool = batch.SolvePool(workers=args.workers, precision=args.precision, tuning=tuning)
     t0 = time.perf_counter()
-    res = batch.SolvePool(workers=args.workers, precision=args.precision).run(jobs)
+    res = pool.run(jobs)
     t_pool = time.perf_counter() - t0
     err = [r.error for r in res + seq if r.error]
     dE = max(abs(r.value - q.value) / abs(q.value) for r, q in zip(res, seq))
@@ -655,7 +657,8 @@ def run_batch(args):
     _line(metric="batched_dmrg_solves_per_s", value=v, unit="solves/s", steps=1, warmup=0,
           ms_per_step=t_pool * 1e3, dtype=f"f64 ({args.precision})",
           config={"workload": "j1j2_chain_batch", "chains": len(jobs), "workers": args.workers,
-                  "nsweeps": 6, "cutoff": 1e-10},
+                  "nsweeps": 6, "cutoff": 1e-10, "tuning": tuning or "table"},
+          gpu_launches=pool.launches, launches_per_s=pool.launches / t_pool,
           sequential_fp64={"value": args.sample / t_seq, "unit": "solves/s", "sample": f"chains 0..{args.sample - 1}"},
           speedup_vs_sequential=v / (args.sample / t_seq), max_rel_dE_vs_sequential=dE, errors=err[:3],
           cpu_baseline=cpu)
@@ -829,6 +832,8 @@ def main():
                          "TDVP; batch: 256 J1-J2 chains on a solve pool; serve: Poisson request stream; "
                          "qn: U(1) block-sparse DMRG")
     ap.add_argument("--workers", type=int, default=16)
+    ap.add_argument("--pool-tridiag", type=int, default=0,
+                    help="batch/serve: the workers' reduction path (-1 grid kernel, 2-16 cluster size, 0 the table)")
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--sample", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)

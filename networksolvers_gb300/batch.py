@@ -142,9 +142,14 @@ class SolvePool:
     in precision mode `precision`; `hbm_bytes` caps the summed footprints of the running
     jobs (default: 90 % of the device's free memory at start)."""
 
-    def __init__(self, workers=8, device=0, precision="fp64", hbm_bytes=None, context_factory=None, runner=None):
+    def __init__(self, workers=8, device=0, precision="fp64", hbm_bytes=None, context_factory=None, runner=None,
+                 tuning=None):
         self.workers, self.device, self.precision = int(workers), int(device), precision
         self.hbm_bytes = hbm_bytes
+        # per-worker launch-choice overrides ({"tridiag": 8, "splitk": 4}, Context.set_tuning):
+        # e.g. smaller clusters for the reductions, so that more solves reduce side by side
+        self.tuning = dict(tuning or {})
+        self.launches = 0  # kernels launched by the workers' contexts in the last run
         # context_factory() -> context with synchronize()/close(); runner(job, ctx) -> value.
         # Defaults: a library context per worker and the DMRG / TDVP drivers.
         self._make_ctx = context_factory or (lambda: _native.Context(self.device, precision=self.precision))
@@ -193,6 +198,8 @@ class SolvePool:
             ctx = self._make_ctx()
             if isinstance(ctx, _native.Context):
                 _native.set_thread_context(ctx)
+                for param, value in self.tuning.items():
+                    ctx.set_tuning(param, value)
             try:
                 while True:
                     i = take()
@@ -212,8 +219,13 @@ class SolvePool:
                     done(i)
             finally:
                 _native.set_thread_context(None)
+                if isinstance(ctx, _native.Context):
+                    n = ctx.counters()["launches"]
+                    with lock:
+                        self.launches += n
                 ctx.close()
 
+        self.launches = 0
         threads = [threading.Thread(target=worker, args=(w,), daemon=True) for w in range(self.workers)]
         for t in threads:
             t.start()

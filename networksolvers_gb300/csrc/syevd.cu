@@ -95,26 +95,34 @@ struct Barrier {
   int err;
 };
 
+// Householder scalars of a pivot column whose first entry below the diagonal is alpha
+// and whose further entries have squared norm xnorm2: beta = -sign(Re alpha) times the
+// column's norm, tau = (beta - alpha) / beta and the scale 1 / (alpha - beta) that turns
+// the column into the reflector v (v[0] = 1).  A zero tail under a real alpha needs no
+// reflection (tau = 0, beta = alpha).
 template <typename T>
-__device__ T block_sum(T v, T* red) {
-  // sum over the block; result valid in every thread
-  for (int o = 16; o > 0; o >>= 1) {
-    if constexpr (sizeof(T) == 8) {
-      v += __shfl_down_sync(0xffffffffu, v, o);
+__device__ __forceinline__ void hh_scalars(T alpha, double xnorm2, T& tk, T& scale, double& beta, bool& active) {
+  const double ar = cre(alpha);
+  double ai = 0.0;
+  if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
+  tk = czero<T>();
+  scale = czero<T>();
+  beta = ar;
+  active = !(xnorm2 == 0.0 && ai == 0.0);
+  if (active) {
+    const double nrm = sqrt(ar * ar + ai * ai + xnorm2);
+    beta = ar >= 0 ? -nrm : nrm;
+    if constexpr (sizeof(T) == 16) {
+      double2 t2 = make_double2((beta - ar) / beta, -ai / beta);
+      tk = *(T*)&t2;
+      double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
+      scale = *(T*)&inv;
     } else {
-      double2 t;
-      t.x = __shfl_down_sync(0xffffffffu, ((double2&)v).x, o);
-      t.y = __shfl_down_sync(0xffffffffu, ((double2&)v).y, o);
-      v = cadd(v, *(T*)&t);
+      double t1 = (beta - ar) / beta, s1 = 1.0 / (ar - beta);
+      tk = *(T*)&t1;
+      scale = *(T*)&s1;
     }
   }
-  __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-  __syncthreads();
-  T s = czero<T>();
-  for (int k = 0; k < int(blockDim.x + 31) / 32; ++k) s = cadd(s, red[k]);
-  __syncthreads();
-  return s;
 }
 
 // Householder tridiagonalisation of the Hermitian n x n matrix A (column-major, both
@@ -141,6 +149,9 @@ __global__ void __launch_bounds__(NT)
   __shared__ double2 wsum[NT / 32];
   __shared__ T part_s[kTriUnits];  // per-unit partial dot products of the pass
   __shared__ int s_ok;
+  __shared__ T s_tk, s_scale, s_alpha2;  // the step's scalars, formed by one thread
+  __shared__ double s_beta;
+  __shared__ bool s_active;
   constexpr int nt = NT, nwarps = NT / 32;
   constexpr bool cplx = sizeof(T) == 16;   // real data: the imaginary halves are never formed
   constexpr int P = (cplx ? 1024 : 2048) / NT;  // pivot-column and x entries per thread held in registers
@@ -208,37 +219,28 @@ __global__ void __launch_bounds__(NT)
       vcur[r] = a;
       ss += cabs2(a);
     }
-    const double xnorm2 = block_sum<double>(ss, (double*)red);  // its barriers publish vcur
-    const T alpha = vcur[0];
-    const double ar = cre(alpha);
-    double ai = 0.0;
-    if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
-    T tk = czero<T>();
-    double beta = ar;
-    T scale = czero<T>();
-    const bool active = !(xnorm2 == 0.0 && ai == 0.0);
-    if (active) {
-      double nrm = sqrt(ar * ar + ai * ai + xnorm2);
-      beta = ar >= 0 ? -nrm : nrm;
-      if constexpr (sizeof(T) == 16) {
-        double2 t2 = make_double2((beta - ar) / beta, -ai / beta);
-        tk = *(T*)&t2;
-        double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
-        scale = *(T*)&inv;
-      } else {
-        double t1 = (beta - ar) / beta, s1 = 1.0 / (ar - beta);
-        tk = *(T*)&t1;
-        scale = *(T*)&s1;
+    // the squared norm: warp sums, then one thread adds them in warp order and forms the
+    // reflector's scalars alone.  A warp-wide FP64 instruction holds a sub-partition's
+    // FP64 pipe for ~64 cycles on this GPU: a scalar chain (square root, two divides)
+    // repeated by every warp would take the CTA's FP64 issue for a step of its own.
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, o);
+    if (lane == 0) ((double*)red)[warp] = ss;
+    __syncthreads();  // publishes vcur and the warp sums
+    if (tid == 0) {
+      double xnorm2 = 0.0;
+      for (int w = 0; w < nwarps; ++w) xnorm2 += ((double*)red)[w];
+      hh_scalars(vcur[0], xnorm2, s_tk, s_scale, s_beta, s_active);
+      if (b == 0) {
+        d[k] = cre(dk);
+        e[k] = s_active ? s_beta : cre(vcur[0]);
+        tau[k] = s_tk;
       }
     }
-    __syncthreads();  // every thread has read vcur[0]
+    __syncthreads();
+    const T tk = s_tk, scale = s_scale;
+    const bool active = s_active;
     for (int r = tid; r < m; r += nt) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scale);
     __syncthreads();
-    if (b == 0 && tid == 0) {
-      d[k] = cre(dk);
-      e[k] = active ? beta : ar;
-      tau[k] = tk;
-    }
     // 2. the pass: pending update, then x_j = tau * A22[:, j]^H v.  A warp loads its next
     //    unit before it updates and stores the current one (units are disjoint).  The
     //    trailing block is rewritten by other CTAs between steps: every access bypasses L1.
@@ -349,10 +351,12 @@ __global__ void __launch_bounds__(NT)
       xr[j] = r < m ? __ldcg(xb + r) : czero<T>();
     }
     double2 pq[PQ];
+    if (warp == 0) {
 #pragma unroll
-    for (int j = 0; j < PQ; ++j) {
-      const int q = lane + 32 * j;
-      pq[j] = q < nact ? __ldcg(pb + q) : make_double2(0.0, 0.0);
+      for (int j = 0; j < PQ; ++j) {
+        const int q = lane + 32 * j;
+        pq[j] = q < nact ? __ldcg(pb + q) : make_double2(0.0, 0.0);
+      }
     }
     {
       const T* coln = A + (size_t)(k + 1) * n + (k + 2);
@@ -364,31 +368,37 @@ __global__ void __launch_bounds__(NT)
       if (b == 0 && tid == 0) rawd = __ldcg(A + (size_t)(k + 1) * n + (k + 1));
     }
     for (int r = tid + P * nt; r < m; r += nt) wprev[r] = __ldcg(xb + r);
-    // every warp sums the CTAs' partials (lane-strided in ascending order, then a
-    // butterfly: the same value in every lane of every CTA)
-    double2 xv = make_double2(0.0, 0.0);
+    // warp 0 sums the CTAs' partials (lane-strided in ascending order, then a butterfly:
+    // the same value in every CTA) and forms alpha2 for the CTA
+    if (warp == 0) {
+      double2 xv = make_double2(0.0, 0.0);
 #pragma unroll
-    for (int j = 0; j < PQ; ++j) {
-      xv.x += pq[j].x;
-      if constexpr (cplx) xv.y += pq[j].y;
+      for (int j = 0; j < PQ; ++j) {
+        xv.x += pq[j].x;
+        if constexpr (cplx) xv.y += pq[j].y;
+      }
+      for (int q = lane + 32 * PQ; q < nact; q += 32) {
+        const double2 t = __ldcg(pb + q);
+        xv.x += t.x;
+        if constexpr (cplx) xv.y += t.y;
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        xv.x += __shfl_xor_sync(0xffffffffu, xv.x, o);
+        if constexpr (cplx) xv.y += __shfl_xor_sync(0xffffffffu, xv.y, o);
+      }
+      if (lane == 0) {
+        T xvT;
+        if constexpr (sizeof(T) == 8) {
+          double t1 = xv.x;
+          xvT = *(T*)&t1;
+        } else {
+          xvT = *(T*)&xv;
+        }
+        s_alpha2 = cscale(cmulv(tk, xvT), -0.5);
+      }
     }
-    for (int q = lane + 32 * PQ; q < nact; q += 32) {
-      const double2 t = __ldcg(pb + q);
-      xv.x += t.x;
-      if constexpr (cplx) xv.y += t.y;
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      xv.x += __shfl_xor_sync(0xffffffffu, xv.x, o);
-      if constexpr (cplx) xv.y += __shfl_xor_sync(0xffffffffu, xv.y, o);
-    }
-    T xvT;
-    if constexpr (sizeof(T) == 8) {
-      double t1 = xv.x;
-      xvT = *(T*)&t1;
-    } else {
-      xvT = *(T*)&xv;
-    }
-    const T alpha2 = cscale(cmulv(tk, xvT), -0.5);
+    __syncthreads();
+    const T alpha2 = s_alpha2;
     // reflector storage below the subdiagonal of column k: every CTA has read column k
     // before the barrier, and it is not read again
     if (b == 0)
@@ -469,16 +479,14 @@ __global__ void __launch_bounds__(kClusterTriThreads)
     for (int r = tid; r < n; r += blockDim.x) cols[(size_t)q * n + r] = src[r];
   }
   cluster.sync();
-  auto bsum_d = [&](double v) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    __syncthreads();
-    if (lane == 0) redd[warp] = v;
-    __syncthreads();
-    double s = 0.0;
-    for (int w = 0; w < NW; ++w) s += redd[w];
-    return s;
-  };
-  auto bsum_t = [&](T v) {
+  // block sums end in one thread (the warps' sums added in warp order), which also forms
+  // the step's scalars: on this GPU a warp-wide FP64 instruction holds a sub-partition's
+  // FP64 pipe for ~64 cycles, so a scalar chain repeated by every warp would take the
+  // CTA's FP64 issue for a step of its own
+  __shared__ T s_tk, s_scl, s_alpha2;
+  __shared__ double s_beta;
+  __shared__ bool s_active;
+  auto warp_sum_t = [&](T v) {
     for (int o = 16; o > 0; o >>= 1) {
       if constexpr (sizeof(T) == 8) {
         v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -489,12 +497,7 @@ __global__ void __launch_bounds__(kClusterTriThreads)
         v = cadd(v, *(T*)&t2);
       }
     }
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    T s = czero<T>();
-    for (int w = 0; w < NW; ++w) s = cadd(s, red[w]);
-    return s;
+    return v;
   };
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;
@@ -507,40 +510,25 @@ __global__ void __launch_bounds__(kClusterTriThreads)
       vcur[r] = a;
       if (r > 0) ss += cabs2(a);
     }
-    T dk = czero<T>();
-    if (rank == owner && tid == 0) dk = pcol[k];
-    const double xnorm2 = bsum_d(ss);  // its barriers publish vcur
-    const T alpha = vcur[0];
-    const double ar = cre(alpha);
-    double ai = 0.0;
-    if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
-    T tk = czero<T>();
-    double beta = ar;
-    T scl = czero<T>();
-    const bool active = !(xnorm2 == 0.0 && ai == 0.0);
-    if (active) {
-      const double nrm = sqrt(ar * ar + ai * ai + xnorm2);
-      beta = ar >= 0 ? -nrm : nrm;
-      if constexpr (sizeof(T) == 16) {
-        double2 t2 = make_double2((beta - ar) / beta, -ai / beta);
-        tk = *(T*)&t2;
-        double2 inv = cdiv(make_double2(1.0, 0.0), make_double2(ar - beta, ai));
-        scl = *(T*)&inv;
-      } else {
-        double t1 = (beta - ar) / beta, s1 = 1.0 / (ar - beta);
-        tk = *(T*)&t1;
-        scl = *(T*)&s1;
+    for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
+    if (lane == 0) redd[warp] = ss;
+    __syncthreads();  // publishes vcur and the warp sums
+    if (tid == 0) {
+      double xnorm2 = 0.0;
+      for (int w = 0; w < NW; ++w) xnorm2 += redd[w];
+      hh_scalars(vcur[0], xnorm2, s_tk, s_scl, s_beta, s_active);
+      if (rank == owner) {
+        d[k] = cre(pcol[k]);
+        e[k] = s_active ? s_beta : cre(vcur[0]);
+        tau[k] = s_tk;
       }
     }
-    __syncthreads();  // every thread has read vcur[0]
+    __syncthreads();
+    const T tk = s_tk, scl = s_scl;
+    const bool active = s_active;
     for (int r = tid; r < m; r += blockDim.x) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scl);
     __syncthreads();
     if (rank == owner) {
-      if (tid == 0) {
-        d[k] = cre(dk);
-        e[k] = active ? beta : ar;
-        tau[k] = tk;
-      }
       T* gcol = A + (size_t)k * n + (k + 1);
       for (int r = tid + 1; r < m; r += blockDim.x) gcol[r] = vcur[r];
     }
@@ -581,8 +569,16 @@ __global__ void __launch_bounds__(kClusterTriThreads)
         xall[r] = xj;
         pv = cadd(pv, cmulv(cconj(xj), vcur[r]));
       }
-      const T xv = bsum_t(pv);
-      const T alpha2 = cscale(cmulv(tk, xv), -0.5);
+      pv = warp_sum_t(pv);
+      if (lane == 0) red[warp] = pv;
+      __syncthreads();
+      if (tid == 0) {
+        T xv = czero<T>();
+        for (int w = 0; w < NW; ++w) xv = cadd(xv, red[w]);
+        s_alpha2 = cscale(cmulv(tk, xv), -0.5);
+      }
+      __syncthreads();
+      const T alpha2 = s_alpha2;
       for (int r = tid; r < m; r += blockDim.x) wv[r] = cadd(xall[r], cmulv(alpha2, vcur[r]));
       __syncthreads();
       // 4. A22 -= v w^H + w v^H on the own trailing columns
