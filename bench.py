@@ -635,7 +635,7 @@ def run_batch(args):
     t0 = time.perf_counter()
     seq = batch.SolvePool(workers=1, precision="fp64").run(jobs[:args.sample])
     t_seq = time.perf_counter() - t0
-    tuning = {"tridiag": args.pool_tridiag} if args.pool_tridiag else None
+    tuning = {k: v for k, v in (("tridiag", args.pool_tridiag), ("dc_leaf", args.pool_leaf)) if v} or None
     pool = batch.SolvePool(workers=args.workers, precision=args.precision, tuning=tuning)
     t0 = time.perf_counter()
     res = pool.run(jobs)
@@ -833,7 +833,9 @@ def main():
                          "qn: U(1) block-sparse DMRG")
     ap.add_argument("--workers", type=int, default=16)
     ap.add_argument("--pool-tridiag", type=int, default=0,
-                    help="batch/serve: the workers' reduction path (-1 grid kernel, 2-16 cluster size, 0 the table)")
+                    help="batch: the workers' reduction path (-1 grid kernel, 2-16 cluster size, 0 the table)")
+    ap.add_argument("--pool-leaf", type=int, default=0,
+                    help="batch: the workers' divide-and-conquer leaf order (4-32, 0 the default)")
     ap.add_argument("--chains", type=int, default=256)
     ap.add_argument("--sample", type=int, default=16)
     ap.add_argument("--rate", type=float, default=1.0)

@@ -114,9 +114,13 @@ int nsg_ctx_wait_probe(nsg_ctx* ctx, int64_t polls);
  * compiled-in tuning table (no counterpart in the reference).  param NSG_TUNE_SPLITK:
  * number of K slices of the FP64 CUDA-core GEMM (1..64; 0 restores the table);
  * NSG_TUNE_TRIDIAG: the Householder tridiagonalisation's path (-1 the grid-wide kernel,
- * 2/4/8/16 one thread-block cluster of that size where the matrix fits it, 0 the table). */
+ * 2/4/8/16 one thread-block cluster of that size where the matrix fits it, 0 the table);
+ * NSG_TUNE_DC_LEAF: the divide and conquer's leaf order (4..32; 0 the default 8: larger
+ * leaves mean fewer merge levels, so fewer launches and host reads per eigensolve, at a
+ * longer leaf solve; a throughput choice for many concurrent small solves). */
 #define NSG_TUNE_SPLITK 0
 #define NSG_TUNE_TRIDIAG 1
+#define NSG_TUNE_DC_LEAF 2
 int nsg_ctx_set_tuning(nsg_ctx* ctx, int param, int value);
 
 /* ---- tensors ------------------------------------------------------------- */

@@ -56,8 +56,9 @@ const PRECISION = Dict(:fp64 => 0, :tf32x3 => 1, :ozaki => 2, :ozaki8 => 3)
 set_precision!(c::Ctx, p::Symbol) = check(c, @ccall lib.nsg_ctx_set_precision(c.h::Ptr{Cvoid}, PRECISION[p]::Cint)::Cint)
 # pin one launch choice of the compiled-in tuning table for this context (measurement):
 # :splitk => 1..64 K slices of small FP64 products, :tridiag => -1 (grid kernel) or a
-# cluster size 2/4/8/16; 0 returns to the table
-const TUNING = Dict(:splitk => 0, :tridiag => 1)
+# cluster size 2/4/8/16, :dc_leaf => divide-and-conquer leaf order 4..32; 0 returns to
+# the table
+const TUNING = Dict(:splitk => 0, :tridiag => 1, :dc_leaf => 2)
 set_tuning!(c::Ctx, p::Symbol, v::Integer) =
   check(c, @ccall lib.nsg_ctx_set_tuning(c.h::Ptr{Cvoid}, TUNING[p]::Cint, Cint(v)::Cint)::Cint)
 

@@ -154,8 +154,9 @@ class Context:
 
     def set_tuning(self, param, value):
         """Launch-choice override (0 restores the compiled-in tuning table): param
-        "splitk" (FP64 GEMM K slices, 1..64) or "tridiag" (-1 grid kernel, 2..16 cluster)."""
-        code = {"splitk": 0, "tridiag": 1}[param]
+        "splitk" (FP64 GEMM K slices, 1..64), "tridiag" (-1 grid kernel, 2..16 cluster)
+        or "dc_leaf" (divide and conquer leaf order, 4..32)."""
+        code = {"splitk": 0, "tridiag": 1, "dc_leaf": 2}[param]
         self.check(self.L.nsg_ctx_set_tuning(self.h, code, int(value)))
 
     def profile(self, enable):

@@ -160,6 +160,9 @@ int nsg_ctx_set_tuning(nsg_ctx* c, int param, int value) {
     NSG_CHECK(value == 0 || value == -1 || value == 2 || value == 4 || value == 8 || value == 16, NSG_ERR_INVALID,
               "tuning: tridiagonalisation path -1, 0, 2, 4, 8 or 16");
     c->tune_tri = value;
+  } else if (param == NSG_TUNE_DC_LEAF) {
+    NSG_CHECK(value == 0 || (value >= 4 && value <= 32), NSG_ERR_INVALID, "tuning: leaf order 0 or 4..32");
+    c->tune_dc_leaf = value;
   } else {
     NSG_CHECK(false, NSG_ERR_INVALID, "tuning: unknown parameter");
   }

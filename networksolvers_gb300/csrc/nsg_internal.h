@@ -60,6 +60,7 @@ struct nsg_ctx {
   // launch-choice overrides set by nsg_ctx_set_tuning (0: the compiled-in tuning table)
   int tune_splitk = 0;  // FP64 GEMM K slices (> 0 forces that count)
   int tune_tri = 0;     // tridiagonalisation: -1 grid kernel, 2..16 cluster size
+  int tune_dc_leaf = 0; // divide and conquer leaf order (4..32; 0 the default)
   // pinned host staging for scalar readback
   double* host_scalars = nullptr;
   size_t host_scalars_cap = 0;

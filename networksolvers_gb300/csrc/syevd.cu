@@ -125,6 +125,48 @@ __device__ __forceinline__ void hh_scalars(T alpha, double xnorm2, T& tk, T& sca
   }
 }
 
+// hh_scalars by one warp, its quotients spread over lanes (each lane runs the same
+// division on its own operands: one division sequence instead of two, or four for
+// complex data); lane 0 stores the results.  Same values as hh_scalars.
+template <typename T>
+__device__ __forceinline__ void hh_scalars_warp(T alpha, double xnorm2, int lane, T& tk, T& scale, double& beta,
+                                                bool& active) {
+  const double ar = cre(alpha);
+  double ai = 0.0;
+  if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
+  const bool act = !(xnorm2 == 0.0 && ai == 0.0);
+  double bt = ar;
+  T t = czero<T>(), s = czero<T>();
+  if (act) {
+    const double nrm = sqrt(ar * ar + ai * ai + xnorm2);
+    bt = ar >= 0 ? -nrm : nrm;
+    if constexpr (sizeof(T) == 16) {
+      // tau = ((beta - ar) / beta, -ai / beta), scale = 1 / (ar - beta + i ai)
+      const double zx = ar - bt, zy = ai;
+      const double den = zx * zx + zy * zy;
+      const double num = lane == 0 ? bt - ar : lane == 1 ? -ai : lane == 2 ? zx : -zy;
+      const double dv = lane < 2 ? bt : den;
+      const double qv = num / dv;
+      const double q0 = __shfl_sync(0xffffffffu, qv, 0), q1 = __shfl_sync(0xffffffffu, qv, 1);
+      const double q2 = __shfl_sync(0xffffffffu, qv, 2), q3 = __shfl_sync(0xffffffffu, qv, 3);
+      double2 t2 = make_double2(q0, q1), s2 = make_double2(q2, q3);
+      t = *(T*)&t2;
+      s = *(T*)&s2;
+    } else {
+      const double qv = (lane == 0 ? bt - ar : 1.0) / (lane == 0 ? bt : ar - bt);
+      const double q0 = __shfl_sync(0xffffffffu, qv, 0), q1 = __shfl_sync(0xffffffffu, qv, 1);
+      t = *(T*)&q0;
+      s = *(T*)&q1;
+    }
+  }
+  if (lane == 0) {
+    tk = t;
+    scale = s;
+    beta = bt;
+    active = act;
+  }
+}
+
 // Householder tridiagonalisation of the Hermitian n x n matrix A (column-major, both
 // triangles stored).  On exit d[k] = T_kk, e[k] = T_k,k+1 (real), tau[k], the reflector
 // vectors v_k (v_k[k+1] = 1 implicit) below the subdiagonal of column k, and
@@ -149,7 +191,8 @@ __global__ void __launch_bounds__(NT)
   __shared__ double2 wsum[NT / 32];
   __shared__ T part_s[kTriUnits];  // per-unit partial dot products of the pass
   __shared__ int s_ok;
-  __shared__ T s_tk, s_scale, s_alpha2;  // the step's scalars, formed by one thread
+  __shared__ T a0_s[kTriUnits];    // first entry (row k+1) of each own column after the update
+  __shared__ T s_tk, s_scale, s_alpha2;  // the step's scalars, formed by one warp
   __shared__ double s_beta;
   __shared__ bool s_active;
   constexpr int nt = NT, nwarps = NT / 32;
@@ -219,31 +262,32 @@ __global__ void __launch_bounds__(NT)
       vcur[r] = a;
       ss += cabs2(a);
     }
-    // the squared norm: warp sums, then one thread adds them in warp order and forms the
-    // reflector's scalars alone.  A warp-wide FP64 instruction holds a sub-partition's
-    // FP64 pipe for ~64 cycles on this GPU: a scalar chain (square root, two divides)
-    // repeated by every warp would take the CTA's FP64 issue for a step of its own.
+    // the squared norm: warp sums, then warp 0 adds them in warp order and forms the
+    // reflector's scalars while the other warps start the pass (a warp-wide FP64
+    // instruction holds a sub-partition's FP64 pipe for ~64 cycles on this GPU: the
+    // scalar chain of square root and divides runs once per CTA, beside the pass).  The
+    // pass needs no scalar: with v_0 = 1 and v_i = scale a_i (i > 0), where
+    // alpha - beta = 1 / scale, A^H v = scale (A^H a - beta conj(A_0,:)); it forms A^H a
+    // with the column as it is and keeps each column's first entry (a0_s).
     for (int o = 16; o > 0; o >>= 1) ss += __shfl_down_sync(0xffffffffu, ss, o);
     if (lane == 0) ((double*)red)[warp] = ss;
-    __syncthreads();  // publishes vcur and the warp sums
-    if (tid == 0) {
+    __syncthreads();  // publishes vcur (the column a, unscaled) and the warp sums
+    if (warp == 0) {
       double xnorm2 = 0.0;
       for (int w = 0; w < nwarps; ++w) xnorm2 += ((double*)red)[w];
-      hh_scalars(vcur[0], xnorm2, s_tk, s_scale, s_beta, s_active);
-      if (b == 0) {
+      hh_scalars_warp(vcur[0], xnorm2, lane, s_tk, s_scale, s_beta, s_active);
+      if (b == 0 && lane == 0) {
         d[k] = cre(dk);
         e[k] = s_active ? s_beta : cre(vcur[0]);
         tau[k] = s_tk;
       }
     }
-    __syncthreads();
-    const T tk = s_tk, scale = s_scale;
-    const bool active = s_active;
-    for (int r = tid; r < m; r += nt) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scale);
-    __syncthreads();
-    // 2. the pass: pending update, then x_j = tau * A22[:, j]^H v.  A warp loads its next
-    //    unit before it updates and stores the current one (units are disjoint).  The
-    //    trailing block is rewritten by other CTAs between steps: every access bypasses L1.
+    // 2. the pass: pending update, then the dot products of the columns with a.  A warp
+    //    loads its next unit before it updates and stores the current one (units are
+    //    disjoint).  The trailing block is rewritten by other CTAs between steps: every
+    //    access bypasses L1.
+    T tk, scale;
+    bool active;
     {
       for (int u = warp; u < nunits; u += nwarps) {
         if (u + nwarps < nunits) load_unit(u + nwarps, nxt);
@@ -261,6 +305,7 @@ __global__ void __launch_bounds__(NT)
               val = fnms2(val, vprev[r + 1], wj, wprev[r + 1], vj);
               __stcg(cj + r, val);
             }
+            if (t == 0 && r == 0) a0_s[q] = val;
             if (t & 1)
               acc1 = fcma(acc1, val, vcur[r]);
             else
@@ -282,7 +327,12 @@ __global__ void __launch_bounds__(NT)
 #pragma unroll
         for (int t = 0; t < U; ++t) cur[t] = nxt[t];
       }
-      __syncthreads();
+      __syncthreads();  // publishes the partial sums, a0_s and the scalars
+      tk = s_tk;
+      scale = s_scale;
+      active = s_active;
+      const double beta = s_beta;
+      const T ts = cmulv(tk, scale);
       // column sums in a fixed order, x, and this CTA's share of x^H v (a warp whose
       // threads own no column contributes nothing and skips its reduction)
       const int cwarps = (ncol + 31) / 32;
@@ -291,9 +341,10 @@ __global__ void __launch_bounds__(NT)
         for (int q = tid; q < ncol; q += nt) {
           T sum = czero<T>();
           for (int rb = 0; rb < nrb; ++rb) sum = cadd(sum, part_s[q * nrb + rb]);
-          const T xi = cmulv(tk, sum);
+          const T xi = cmulv(ts, csub(sum, cscale(cconj(a0_s[q]), beta)));
           __stcg(xb + j0 + q, xi);
-          const T p = cmulv(cconj(xi), vcur[j0 + q]);
+          const T vq = (j0 + q == 0) ? cone<T>() : cmulv(scale, vcur[j0 + q]);
+          const T p = cmulv(cconj(xi), vq);
           if constexpr (!cplx) {
             pacc.x += (double&)p;
           } else {
@@ -308,6 +359,8 @@ __global__ void __launch_bounds__(NT)
         if (lane == 0) wsum[warp] = pacc;
       }
       __syncthreads();
+      // the reflector v itself (v_0 = 1) for the update, its storage and the next step
+      for (int r = tid; r < m; r += nt) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scale);
       if (tid == 0) {
         double2 sacc = cwarps > 0 ? wsum[0] : make_double2(0.0, 0.0);
         for (int w = 1; w < cwarps; ++w) {
@@ -479,7 +532,7 @@ __global__ void __launch_bounds__(kClusterTriThreads)
     for (int r = tid; r < n; r += blockDim.x) cols[(size_t)q * n + r] = src[r];
   }
   cluster.sync();
-  // block sums end in one thread (the warps' sums added in warp order), which also forms
+  // block sums end in one warp (the warps' sums added in warp order), which also forms
   // the step's scalars: on this GPU a warp-wide FP64 instruction holds a sub-partition's
   // FP64 pipe for ~64 cycles, so a scalar chain repeated by every warp would take the
   // CTA's FP64 issue for a step of its own
@@ -512,54 +565,63 @@ __global__ void __launch_bounds__(kClusterTriThreads)
     }
     for (int o = 16; o > 0; o >>= 1) ss += __shfl_xor_sync(0xffffffffu, ss, o);
     if (lane == 0) redd[warp] = ss;
-    __syncthreads();  // publishes vcur and the warp sums
-    if (tid == 0) {
+    __syncthreads();  // publishes vcur (the column a, unscaled) and the warp sums
+    // warp 0 forms the reflector's scalars while the other warps form the dot products
+    // S_j = sum_i conj(A_ij) a_i of the own trailing columns with the column as it is
+    // (one warp per column): with v_0 = 1, v_i = scale a_i (i > 0) and
+    // alpha - beta = 1 / scale, A^H v = scale (S - beta conj(A_0,:))
+    if (warp == 0) {
       double xnorm2 = 0.0;
       for (int w = 0; w < NW; ++w) xnorm2 += redd[w];
-      hh_scalars(vcur[0], xnorm2, s_tk, s_scl, s_beta, s_active);
-      if (rank == owner) {
+      hh_scalars_warp(vcur[0], xnorm2, lane, s_tk, s_scl, s_beta, s_active);
+      if (rank == owner && lane == 0) {
         d[k] = cre(pcol[k]);
         e[k] = s_active ? s_beta : cre(vcur[0]);
         tau[k] = s_tk;
       }
     }
-    __syncthreads();
+    // 2. x_j = tau sum_i conj(A_ij) v_i for the own trailing columns
+    const int q0 = (k + 1 - rank + C - 1) / C;  // first own column index with j >= k+1
+    for (int q = q0 + warp; q < ncol; q += NW) {
+      const int j = rank + C * q;
+      const T* cj = cols + (size_t)q * n + (k + 1);
+      T acc = czero<T>(), acc1 = czero<T>();
+      int r = lane;
+      for (; r + 32 < m; r += 64) {
+        acc = fcma(acc, cj[r], vcur[r]);
+        acc1 = fcma(acc1, cj[r + 32], vcur[r + 32]);
+      }
+      if (r < m) acc = fcma(acc, cj[r], vcur[r]);
+      acc = cadd(acc, acc1);
+      for (int o = 16; o > 0; o >>= 1) {
+        if constexpr (sizeof(T) == 8) {
+          acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        } else {
+          double2 t2;
+          t2.x = __shfl_xor_sync(0xffffffffu, ((double2&)acc).x, o);
+          t2.y = __shfl_xor_sync(0xffffffffu, ((double2&)acc).y, o);
+          acc = cadd(acc, *(T*)&t2);
+        }
+      }
+      if (lane == 0) xloc[j] = acc;
+    }
+    __syncthreads();  // publishes the scalars and the dot products
     const T tk = s_tk, scl = s_scl;
     const bool active = s_active;
+    {
+      const double beta = s_beta;
+      const T ts = cmulv(tk, scl);
+      for (int q = q0 + tid; q < ncol; q += blockDim.x) {
+        const int j = rank + C * q;
+        xloc[j] = cmulv(ts, csub(xloc[j], cscale(cconj(cols[(size_t)q * n + (k + 1)]), beta)));
+      }
+    }
     for (int r = tid; r < m; r += blockDim.x) vcur[r] = (r == 0) ? cone<T>() : cmulv(vcur[r], scl);
-    __syncthreads();
+    cluster.sync();  // publishes x to the peers and the scaled reflector within the CTA
     if (rank == owner) {
       T* gcol = A + (size_t)k * n + (k + 1);
       for (int r = tid + 1; r < m; r += blockDim.x) gcol[r] = vcur[r];
     }
-    // 2. x_j = tau sum_i conj(A_ij) v_i for the own trailing columns (one warp per column)
-    const int q0 = (k + 1 - rank + C - 1) / C;  // first own column index with j >= k+1
-    if (active) {
-      for (int q = q0 + warp; q < ncol; q += NW) {
-        const int j = rank + C * q;
-        const T* cj = cols + (size_t)q * n + (k + 1);
-        T acc = czero<T>(), acc1 = czero<T>();
-        int r = lane;
-        for (; r + 32 < m; r += 64) {
-          acc = fcma(acc, cj[r], vcur[r]);
-          acc1 = fcma(acc1, cj[r + 32], vcur[r + 32]);
-        }
-        if (r < m) acc = fcma(acc, cj[r], vcur[r]);
-        acc = cadd(acc, acc1);
-        for (int o = 16; o > 0; o >>= 1) {
-          if constexpr (sizeof(T) == 8) {
-            acc += __shfl_xor_sync(0xffffffffu, acc, o);
-          } else {
-            double2 t2;
-            t2.x = __shfl_xor_sync(0xffffffffu, ((double2&)acc).x, o);
-            t2.y = __shfl_xor_sync(0xffffffffu, ((double2&)acc).y, o);
-            acc = cadd(acc, *(T*)&t2);
-          }
-        }
-        if (lane == 0) xloc[j] = cmulv(tk, acc);
-      }
-    }
-    cluster.sync();
     if (active) {
       // 3. gather x, x^H v, w = x - tau/2 (x^H v) v
       T pv = czero<T>();
@@ -779,7 +841,6 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
   int* pm = sm ? (int*)(zsm + nb) : W.perm + lo;
   int* kd = sm ? pm + nb : W.kind + lo;
   __shared__ double red[32], redm[32];
-  __shared__ int s_nrot;
   for (int li = threadIdx.x; li < nb; li += blockDim.x) {
     ws[li] = w[lo + li];
     zr[li] = (li < n1) ? Q[(size_t)(lo + li) * n + (mid - 1)] : Q[(size_t)(lo + li) * n + mid];
@@ -882,7 +943,6 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
     W.counts[3 * mi] = k;
     W.counts[3 * mi + 1] = nrot;
     W.counts[3 * mi + 2] = flip;
-    s_nrot = nrot;
   }
   __syncthreads();
   if (sm) {
@@ -893,7 +953,6 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
       W.kind[lo + t] = kd[t];
     }
   }
-  (void)s_nrot;
 }
 
 // The deflation rotations of every merge of a level, in order, on the block's columns of
@@ -1290,17 +1349,9 @@ static void build_tree(int lo, int hi, std::vector<std::vector<MergeDesc>>& leve
 
 // Leaf order of the divide and conquer: the implicit-QL leaves are one warp each and
 // latency bound (a chain of FP64 square roots and divides per rotation), so small leaves
-// and more (batched) merge levels are cheaper.  NSG_DC_LEAF (4..32) overrides it.
-static int dc_leaf_size(int n) {
-  static int env = [] {
-    const char* s = std::getenv("NSG_DC_LEAF");
-    int v = s ? std::atoi(s) : 0;
-    return (v >= 4 && v <= kLeaf) ? v : 0;
-  }();
-  if (env) return env;
-  (void)n;
-  return 8;
-}
+// and more (batched) merge levels are cheaper for one solve.  The context's override
+// (4..32) trades that latency for fewer levels: fewer launches and host reads.
+static int dc_leaf_size(const nsg_ctx* c) { return c->tune_dc_leaf > 0 ? c->tune_dc_leaf : 8; }
 
 // Eigen-decomposition of the real symmetric tridiagonal (d, e); Q: n x n (device,
 // column-major), w: eigenvalues ascending (device).  Cuppen's divide and conquer with
@@ -1309,7 +1360,7 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
                        double* w) {
   std::vector<std::vector<MergeDesc>> levels;
   std::vector<int> llo, lhi;
-  build_tree(0, n, levels, llo, lhi, 0, dc_leaf_size(n));
+  build_tree(0, n, levels, llo, lhi, 0, dc_leaf_size(c));
   // modified diagonal: for each split subtract beta at the two touching diagonals
   std::vector<double> d = d_in;
   for (auto& lv : levels)
