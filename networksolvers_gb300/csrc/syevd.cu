@@ -823,6 +823,60 @@ struct DcWork {
 
 constexpr int kSmemMerge = 4096;  // rows of a block whose serial steps run in shared memory
 
+// Order-preserving integer key of a double (x < y exactly when key(x) < key(y); -0 and +0
+// equal), so the merges compare with integer instructions rather than the FP64 pipe,
+// and the exact negation -x by its sign bit.
+__device__ __forceinline__ long long order_key(double x) {
+  const long long b = __double_as_longlong(x);
+  if ((b & 0x7fffffffffffffffLL) == 0) return 0;
+  return b < 0 ? (b ^ 0x7fffffffffffffffLL) : b;
+}
+__device__ __forceinline__ double neg_exact(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)(1ULL << 63));
+}
+
+// Exclusive prefix sum of v over the block's threads in thread order (sh: 32 ints);
+// the block total goes to *tot.  Every thread of the block must call it.
+__device__ int block_scan_excl(int v, int* sh, int* tot) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int t = lane < nw ? sh[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    if (lane < nw) sh[lane] = t;
+  }
+  __syncthreads();
+  const int before = warp > 0 ? sh[warp - 1] : 0;
+  *tot = sh[nw - 1];
+  __syncthreads();
+  return before + x - v;
+}
+
+// Number of indices i in [0, len) with key(i) < k (strict) or key(i) <= k, for keys
+// ascending in i.
+template <bool kStrict, typename F>
+__device__ __forceinline__ int rank_in(F key, int len, long long k) {
+  int lo = 0, hi = len;
+  while (lo < hi) {
+    const int md = (lo + hi) >> 1;
+    const long long v = key(md);
+    if (kStrict ? (v < k) : (v <= k))
+      lo = md + 1;
+    else
+      hi = md;
+  }
+  return lo;
+}
+
 // Per merge (one CTA): gather the two halves' eigenvalues and the z vector (last row of
 // block 1, first row of block 2), flip for rho < 0, merge the ascending halves, normalise
 // z, deflate (small z_t; poles closer than tol rotated together), apply the deflation
@@ -841,34 +895,63 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
   int* pm = sm ? (int*)(zsm + nb) : W.perm + lo;
   int* kd = sm ? pm + nb : W.kind + lo;
   __shared__ double red[32], redm[32];
+  __shared__ int scan_sh[32], s_flag, s_nrot;
   for (int li = threadIdx.x; li < nb; li += blockDim.x) {
     ws[li] = w[lo + li];
     zr[li] = (li < n1) ? Q[(size_t)(lo + li) * n + (mid - 1)] : Q[(size_t)(lo + li) * n + mid];
   }
+  if (threadIdx.x == 0) {
+    s_flag = 0;
+    s_nrot = 0;
+  }
   __syncthreads();
   double rho = M.beta;
   const int flip = rho < 0;
-  const double sg = flip ? -1.0 : 1.0;
   if (flip) rho = -rho;
-  if (threadIdx.x == 0) {
-    int a = 0, b = 0;
+  // merge of the two ascending halves (both traversed from their top when flipped, values
+  // negated) into ascending poles; ties take the first half first.  An entry's slot is
+  // its rank in its own half plus its rank in the other, by binary search on integer keys.
+  const int n2 = nb - n1;
+  auto srcA = [&](int a) { return flip ? (n1 - 1 - a) : a; };
+  auto srcB = [&](int b2) { return flip ? (nb - 1 - b2) : (n1 + b2); };
+  auto valA = [&](int a) { return flip ? neg_exact(ws[srcA(a)]) : ws[srcA(a)]; };
+  auto valB = [&](int b2) { return flip ? neg_exact(ws[srcB(b2)]) : ws[srcB(b2)]; };
+  auto keyA = [&](int a) { return order_key(valA(a)); };
+  auto keyB = [&](int b2) { return order_key(valB(b2)); };
+  for (int t = threadIdx.x; t < nb; t += blockDim.x)  // halves out of order: the serial merge
+    if ((t > 0 && t < n1 && keyA(t) < keyA(t - 1)) || (t > n1 && keyB(t - n1) < keyB(t - n1 - 1))) s_flag = 1;
+  __syncthreads();
+  if (!s_flag) {
+    for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+      int pos, li;
+      if (t < n1) {
+        pos = t + rank_in<true>(keyB, n2, keyA(t));
+        li = srcA(t);
+      } else {
+        pos = (t - n1) + rank_in<false>(keyA, n1, keyB(t - n1));
+        li = srcB(t - n1);
+      }
+      pm[pos] = li;
+      Dsm[pos] = flip ? neg_exact(ws[li]) : ws[li];
+      zsm[pos] = zr[li];
+    }
+  } else if (threadIdx.x == 0) {
+    int a = 0, b2 = 0;
     for (int t = 0; t < nb; ++t) {
-      const int ia = flip ? (n1 - 1 - a) : a;
-      const int ib = flip ? (nb - 1 - b) : (n1 + b);
       bool takeA;
       if (a >= n1)
         takeA = false;
-      else if (b >= nb - n1)
+      else if (b2 >= n2)
         takeA = true;
       else
-        takeA = sg * ws[ia] <= sg * ws[ib];
-      const int li = takeA ? ia : ib;
+        takeA = keyA(a) <= keyB(b2);
+      const int li = takeA ? srcA(a) : srcB(b2);
       if (takeA)
         ++a;
       else
-        ++b;
+        ++b2;
       pm[t] = li;
-      Dsm[t] = sg * ws[li];
+      Dsm[t] = flip ? neg_exact(ws[li]) : ws[li];
       zsm[t] = zr[li];
     }
   }
@@ -896,20 +979,33 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
   }
   nz = sqrt(nz);
   rho = rho * nz * nz;
-  for (int t = threadIdx.x; t < nb; t += blockDim.x) zsm[t] /= nz;
+  const double tol = 8.0 * 2.220446049250313e-16 * fmax(dmax, rho);
+  // deflation of small weights (independent per pole), then of poles closer than tol:
+  // the sorted poles' closest kept pair is consecutive among the kept ones, so a pass
+  // that finds none proves that the serial rotation sweep would rotate nothing
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    const double z = zsm[t] / nz;
+    const bool small = rho * fabs(z) <= tol;
+    kd[t] = small ? 0 : 1;
+    zsm[t] = small ? 0.0 : z;
+  }
+  if (threadIdx.x == 0) s_flag = 0;
+  __syncthreads();
+  for (int t = threadIdx.x; t < nb; t += blockDim.x) {
+    if (!kd[t]) continue;
+    for (int u = t + 1; u < nb; ++u)
+      if (kd[u]) {
+        if (fabs(Dsm[u] - Dsm[t]) <= tol) s_flag = 1;
+        break;
+      }
+  }
   __syncthreads();
   int* rpq = W.rot_pq + 2 * lo;
   double* rcs = W.rot_cs + 2 * lo;
-  if (threadIdx.x == 0) {
-    const double tol = 8.0 * 2.220446049250313e-16 * fmax(dmax, rho);
-    int k = 0, nrot = 0, prev = -1;
+  if (s_flag && threadIdx.x == 0) {
+    int nrot = 0, prev = -1;
     for (int t = 0; t < nb; ++t) {
-      if (rho * fabs(zsm[t]) <= tol) {
-        kd[t] = 0;
-        zsm[t] = 0.0;
-        continue;
-      }
-      kd[t] = 1;
+      if (!kd[t]) continue;
       if (prev >= 0 && fabs(Dsm[t] - Dsm[prev]) <= tol) {
         const double r = hypot(zsm[t], zsm[prev]);
         const double c = zsm[t] / r, sn = zsm[prev] / r;
@@ -927,24 +1023,34 @@ __global__ void dc_prep_kernel(const double* __restrict__ w, double* __restrict_
       }
       prev = t;
     }
-    // compaction of the non-deflated slots
+    s_nrot = nrot;
+  }
+  __syncthreads();
+  // compaction of the non-deflated slots (block scan over contiguous chunks)
+  {
+    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    const int c0 = min(nb, (int)threadIdx.x * per), c1 = min(nb, c0 + per);
+    int cnt = 0;
+    for (int t = c0; t < c1; ++t) cnt += kd[t];
+    int k = 0;
+    int off = block_scan_excl(cnt, scan_sh, &k);
     int* kinv = W.kinv + lo;
     double* Dk = W.Dk + lo;
     double* zk = W.zk + lo;
-    for (int t = 0; t < nb; ++t) {
+    for (int t = c0; t < c1; ++t)
       if (kd[t]) {
-        kinv[k] = t;
-        Dk[k] = Dsm[t];
-        zk[k] = zsm[t];
-        ++k;
+        kinv[off] = t;
+        Dk[off] = Dsm[t];
+        zk[off] = zsm[t];
+        ++off;
       }
+    if (threadIdx.x == 0) {
+      W.rho[mi] = rho;
+      W.counts[3 * mi] = k;
+      W.counts[3 * mi + 1] = s_nrot;
+      W.counts[3 * mi + 2] = flip;
     }
-    W.rho[mi] = rho;
-    W.counts[3 * mi] = k;
-    W.counts[3 * mi + 1] = nrot;
-    W.counts[3 * mi + 2] = flip;
   }
-  __syncthreads();
   if (sm) {
     for (int t = threadIdx.x; t < nb; t += blockDim.x) {
       W.Ds[lo + t] = Dsm[t];
@@ -1177,7 +1283,57 @@ __global__ void dc_order_kernel(const MergeDesc* __restrict__ md, DcWork W) {
     for (int t = threadIdx.x; t < nr; t += blockDim.x) lm[t] = W.lam[lo + t];
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  // the deflated slots in order (block scan), then a stable merge of the ascending roots
+  // with the deflated poles (ties: the root first) by ranks on integer keys; poles moved
+  // by a deflation rotation can be out of order by up to the deflation tolerance, and
+  // then the merge is the serial one
+  __shared__ int scan_sh[32], s_unsorted;
+  int* dl = si;  // deflated slots, in the output index array until the outputs are formed
+  {
+    const int per = (nb + blockDim.x - 1) / blockDim.x;
+    const int c0 = min(nb, (int)threadIdx.x * per), c1 = min(nb, c0 + per);
+    int cnt = 0;
+    for (int t = c0; t < c1; ++t) cnt += 1 - kd[t];
+    int tot = 0;
+    int off = block_scan_excl(cnt, scan_sh, &tot);
+    for (int t = c0; t < c1; ++t)
+      if (!kd[t]) dl[off++] = t;
+  }
+  // (each thread keeps its ranks in registers: at most 16 entries of each kind)
+  if (threadIdx.x == 0) s_unsorted = nb > 16 * (int)blockDim.x;
+  __syncthreads();
+  auto keyR = [&](int i) { return order_key(lm[i]); };
+  auto keyD = [&](int j) { return order_key(Dsm[dl[j]]); };
+  for (int i = threadIdx.x + 1; i < nr; i += blockDim.x)
+    if (keyR(i) < keyR(i - 1)) s_unsorted = 1;
+  for (int j = threadIdx.x + 1; j < nd; j += blockDim.x)
+    if (keyD(j) < keyD(j - 1)) s_unsorted = 1;
+  __syncthreads();
+  if (!s_unsorted) {
+    // ranks first (every thread reads dl), then the outputs (which overwrite si = dl)
+    int posr[16], posd[16];
+    int nrl = 0, ndl = 0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) posr[nrl++] = i + rank_in<true>(keyD, nd, keyR(i));
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) posd[ndl++] = j + rank_in<false>(keyR, nr, keyD(j));
+    int slots[16];
+    ndl = 0;
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) slots[ndl++] = dl[j];
+    __syncthreads();
+    nrl = 0;
+    for (int i = threadIdx.x; i < nr; i += blockDim.x) {
+      const int pos = posr[nrl++], out = flip ? (nb - 1 - pos) : pos;
+      sk[out] = 1;
+      si[out] = i;
+      wo[out] = flip ? neg_exact(lm[i]) : lm[i];
+    }
+    ndl = 0;
+    for (int j = threadIdx.x; j < nd; j += blockDim.x) {
+      const int pos = posd[ndl], slot = slots[ndl++], out = flip ? (nb - 1 - pos) : pos;
+      sk[out] = 0;
+      si[out] = slot;
+      wo[out] = flip ? neg_exact(Dsm[slot]) : Dsm[slot];
+    }
+  } else if (threadIdx.x == 0) {
     int ia = 0, ib = 0, pos = 0, dslot = 0;
     while (dslot < nb && kd[dslot]) ++dslot;
     while (ia < nr || ib < nd) {

@@ -419,6 +419,29 @@ def test_eigensolver_large_and_degenerate(nsg_ctx, cplx, m, n, precision):
         assert rel(info["spectrum"][:kref], s[:kref] ** 2) < 1e-12
 
 
+@pytest.mark.parametrize("n", [24, 200, 700])
+def test_eigh_exact_multiplets(nsg_ctx, n):
+    """Spectra with exact multiplets (the Heisenberg chain's SU(2) structure in the extreme)
+    make the divide and conquer deflate by close poles: its rotation sweep and the merges
+    around rotated poles run.  Eigenvalues 1e-12 of the largest, orthonormal eigenvectors,
+    reconstruction of the kept part."""
+    rng = np.random.default_rng(n)
+    mult = rng.integers(1, 6, size=n)
+    lam = np.repeat(np.linspace(1.0, 0.01, n), mult)[:n]
+    lam[rng.random(n) < 0.2] = 0.0  # and an exact null space
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    A = (Q * lam) @ Q.T
+    A = 0.5 * (A + A.T)
+    k = Index(n)
+    T = DTensor.from_numpy(A, [k.prime(), k])
+    D, U, u = it.eigen_hermitian(T, [k], cutoff=0.0, maxdim=n)
+    ref = np.sort(np.linalg.eigvalsh(A))[::-1]
+    assert np.max(np.abs(D - ref[: len(D)])) < 1e-12 * ref[0]
+    Un = U.to_numpy().reshape(n, -1)
+    assert np.abs(Un.T @ Un - np.eye(Un.shape[1])).max() < 1e-12
+    assert np.linalg.norm((Un * D) @ Un.T - A) < 1e-12 * n * np.linalg.norm(A)
+
+
 def test_fused_region_step_matches_call_by_call(nsg_ctx):
     """nsg_region_step (product, Lanczos, truncated factorization in one call) against
     the same region step taken entry point by entry point."""
