@@ -131,9 +131,12 @@ __device__ __forceinline__ void hh_scalars(T alpha, double xnorm2, T& tk, T& sca
 template <typename T>
 __device__ __forceinline__ void hh_scalars_warp(T alpha, double xnorm2, int lane, T& tk, T& scale, double& beta,
                                                 bool& active) {
-  const double ar = cre(alpha);
+  // lane 0's operands for every lane: the branch below holds full-warp shuffles, so it
+  // must be uniform over the warp whatever the caller's lanes hold
+  xnorm2 = __shfl_sync(0xffffffffu, xnorm2, 0);
+  const double ar = __shfl_sync(0xffffffffu, cre(alpha), 0);
   double ai = 0.0;
-  if constexpr (sizeof(T) == 16) ai = ((double2&)alpha).y;
+  if constexpr (sizeof(T) == 16) ai = __shfl_sync(0xffffffffu, ((double2&)alpha).y, 0);
   const bool act = !(xnorm2 == 0.0 && ai == 0.0);
   double bt = ar;
   T t = czero<T>(), s = czero<T>();
@@ -196,6 +199,7 @@ __global__ void __launch_bounds__(NT)
   __shared__ double s_beta;
   __shared__ bool s_active;
   constexpr int nt = NT, nwarps = NT / 32;
+  static_assert(nwarps >= 2 && (nwarps & (nwarps - 1)) == 0, "warp 0 plus pass warps, a power of two");
   constexpr bool cplx = sizeof(T) == 16;   // real data: the imaginary halves are never formed
   constexpr int P = (cplx ? 1024 : 2048) / NT;  // pivot-column and x entries per thread held in registers
   constexpr int PQ = 8;                      // CTA partial sums per lane held in registers
@@ -215,7 +219,8 @@ __global__ void __launch_bounds__(NT)
   if (b == 0 && tid == 0) rawd = __ldcg(A);
   for (int k = 0; k < n - 2; ++k) {
     const int m = n - k - 1;  // trailing size (rows k+1..n-1)
-    int nact = int(((int64_t)m * m + (int64_t)nt * per_thread - 1) / ((int64_t)nt * per_thread));
+    // (32-bit index arithmetic: the order is at most ~8.5k, so m^2 and m x CTAs fit)
+    int nact = (m * m + nt * per_thread - 1) / (nt * per_thread);
     nact = max(1, min(nact, (int)gridDim.x));
     if (b >= nact) return;
     // x and the partial sums are double-buffered by step parity: a CTA that runs ahead
@@ -224,10 +229,14 @@ __global__ void __launch_bounds__(NT)
     T* xb = xbuf + (size_t)(k & 1) * n;
     double2* pb = (double2*)partial + (size_t)(k & 1) * gridDim.x;
     // the CTA's columns [j0, j1) of the trailing block, in work units of one column x RB
-    // rows dealt to the warps round-robin; the block is final since the last barrier, so
-    // each warp's first unit is requested before the pivot column is reduced
-    const int j0 = int((int64_t)m * b / nact), j1 = int((int64_t)m * (b + 1) / nact);
+    // rows dealt round-robin to the pass warps (every warp but warp 0, which forms the
+    // step's scalars meanwhile: their chain of dependent FP64 operations would otherwise
+    // delay warp 0's units); the block is final since the last barrier, so each pass
+    // warp's first unit is requested before the pivot column is reduced
+    const int j0 = m * b / nact, j1 = m * (b + 1) / nact;
     const int ncol = j1 - j0, nrb = (m + RB - 1) / RB, nunits = ncol * nrb;
+    constexpr int PW = nwarps - 1;
+    const int pw = warp - 1;
     T cur[U], nxt[U];
     auto load_unit = [&](int u, T* dst) {
       const int q = u / nrb, rb = u - q * nrb;
@@ -238,14 +247,14 @@ __global__ void __launch_bounds__(NT)
         dst[t] = r < m ? __ldcg(cj + r) : czero<T>();
       }
     };
-    if (warp < nunits) load_unit(warp, cur);
+    if (warp > 0 && pw < nunits) load_unit(pw, cur);
     // 1. pivot column k with the pending update applied (rows k..n-1), reflector
     const T* colk = A + (size_t)k * n;
     const T wp0 = has_prev ? cconj(wprev[0]) : czero<T>();
     const T vp0 = has_prev ? cconj(vprev[0]) : czero<T>();
     T dk = czero<T>();
     if (b == 0 && tid == 0) dk = has_prev ? fnms2(rawd, vprev[0], wp0, wprev[0], vp0) : rawd;
-    double ss = 0.0;
+    double ss = 0.0, ss1 = 0.0;  // two chains of dependent FP64 additions
 #pragma unroll
     for (int j = 0; j < P; ++j) {
       const int r = tid + j * nt;
@@ -253,9 +262,15 @@ __global__ void __launch_bounds__(NT)
         T a = raw[j];
         if (has_prev) a = fnms2(a, vprev[r + 1], wp0, wprev[r + 1], vp0);
         vcur[r] = a;
-        if (r > 0) ss += cabs2(a);
+        if (r > 0) {
+          if (j & 1)
+            ss1 += cabs2(a);
+          else
+            ss += cabs2(a);
+        }
       }
     }
+    ss += ss1;
     for (int r = tid + P * nt; r < m; r += nt) {  // orders above P nt + 1: loaded here
       T a = __ldcg(colk + k + 1 + r);
       if (has_prev) a = fnms2(a, vprev[r + 1], wp0, wprev[r + 1], vp0);
@@ -273,8 +288,10 @@ __global__ void __launch_bounds__(NT)
     if (lane == 0) ((double*)red)[warp] = ss;
     __syncthreads();  // publishes vcur (the column a, unscaled) and the warp sums
     if (warp == 0) {
-      double xnorm2 = 0.0;
-      for (int w = 0; w < nwarps; ++w) xnorm2 += ((double*)red)[w];
+      // a butterfly over all 32 lanes (zeros beyond the warp count): every lane holds the
+      // same total, which hh_scalars_warp's lane-uniform branch and shuffles require
+      double xnorm2 = lane < nwarps ? ((double*)red)[lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) xnorm2 += __shfl_xor_sync(0xffffffffu, xnorm2, o);
       hh_scalars_warp(vcur[0], xnorm2, lane, s_tk, s_scale, s_beta, s_active);
       if (b == 0 && lane == 0) {
         d[k] = cre(dk);
@@ -289,8 +306,8 @@ __global__ void __launch_bounds__(NT)
     T tk, scale;
     bool active;
     {
-      for (int u = warp; u < nunits; u += nwarps) {
-        if (u + nwarps < nunits) load_unit(u + nwarps, nxt);
+      for (int u = warp > 0 ? pw : nunits; u < nunits; u += PW) {
+        if (u + PW < nunits) load_unit(u + PW, nxt);
         const int q = u / nrb, rb = u - q * nrb, jj = j0 + q;
         T* cj = A + (size_t)(k + 1 + jj) * n + (k + 1);
         const T wj = has_prev ? cconj(wprev[jj + 1]) : czero<T>();
@@ -424,12 +441,15 @@ __global__ void __launch_bounds__(NT)
     // warp 0 sums the CTAs' partials (lane-strided in ascending order, then a butterfly:
     // the same value in every CTA) and forms alpha2 for the CTA
     if (warp == 0) {
-      double2 xv = make_double2(0.0, 0.0);
+      // a tree over the lane's partials, then over the lanes
 #pragma unroll
-      for (int j = 0; j < PQ; ++j) {
-        xv.x += pq[j].x;
-        if constexpr (cplx) xv.y += pq[j].y;
-      }
+      for (int h = PQ / 2; h > 0; h >>= 1)
+#pragma unroll
+        for (int j = 0; j < h; ++j) {
+          pq[j].x += pq[j + h].x;
+          if constexpr (cplx) pq[j].y += pq[j + h].y;
+        }
+      double2 xv = pq[0];
       for (int q = lane + 32 * PQ; q < nact; q += 32) {
         const double2 t = __ldcg(pb + q);
         xv.x += t.x;
@@ -527,6 +547,7 @@ __global__ void __launch_bounds__(kClusterTriThreads)
   __shared__ double redd[kClusterTriThreads / 32];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   constexpr int NW = kClusterTriThreads / 32;
+  static_assert(NW >= 2 && (NW & (NW - 1)) == 0, "warp 0 plus dot-product warps, a power of two");
   for (int q = 0; q < ncol; ++q) {
     const T* src = A + (size_t)(rank + C * q) * n;
     for (int r = tid; r < n; r += blockDim.x) cols[(size_t)q * n + r] = src[r];
@@ -571,8 +592,10 @@ __global__ void __launch_bounds__(kClusterTriThreads)
     // (one warp per column): with v_0 = 1, v_i = scale a_i (i > 0) and
     // alpha - beta = 1 / scale, A^H v = scale (S - beta conj(A_0,:))
     if (warp == 0) {
-      double xnorm2 = 0.0;
-      for (int w = 0; w < NW; ++w) xnorm2 += redd[w];
+      // a butterfly over all 32 lanes (zeros beyond the warp count): every lane holds the
+      // same total, which hh_scalars_warp's lane-uniform branch and shuffles require
+      double xnorm2 = lane < NW ? redd[lane] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) xnorm2 += __shfl_xor_sync(0xffffffffu, xnorm2, o);
       hh_scalars_warp(vcur[0], xnorm2, lane, s_tk, s_scl, s_beta, s_active);
       if (rank == owner && lane == 0) {
         d[k] = cre(pcol[k]);
@@ -580,9 +603,10 @@ __global__ void __launch_bounds__(kClusterTriThreads)
         tau[k] = s_tk;
       }
     }
-    // 2. x_j = tau sum_i conj(A_ij) v_i for the own trailing columns
+    // 2. x_j = tau sum_i conj(A_ij) v_i for the own trailing columns, one warp per column
+    //    on the warps other than warp 0
     const int q0 = (k + 1 - rank + C - 1) / C;  // first own column index with j >= k+1
-    for (int q = q0 + warp; q < ncol; q += NW) {
+    for (int q = warp > 0 ? q0 + warp - 1 : ncol; q < ncol; q += NW - 1) {
       const int j = rank + C * q;
       const T* cj = cols + (size_t)q * n + (k + 1);
       T acc = czero<T>(), acc1 = czero<T>();
@@ -634,10 +658,19 @@ __global__ void __launch_bounds__(kClusterTriThreads)
       pv = warp_sum_t(pv);
       if (lane == 0) red[warp] = pv;
       __syncthreads();
-      if (tid == 0) {
-        T xv = czero<T>();
-        for (int w = 0; w < NW; ++w) xv = cadd(xv, red[w]);
-        s_alpha2 = cscale(cmulv(tk, xv), -0.5);
+      if (warp == 0) {
+        T xv = lane < NW ? red[lane] : czero<T>();  // a butterfly over the lanes
+        for (int o = 16; o > 0; o >>= 1) {
+          if constexpr (sizeof(T) == 8) {
+            xv += __shfl_xor_sync(0xffffffffu, xv, o);
+          } else {
+            double2 t2;
+            t2.x = __shfl_xor_sync(0xffffffffu, ((double2&)xv).x, o);
+            t2.y = __shfl_xor_sync(0xffffffffu, ((double2&)xv).y, o);
+            xv = cadd(xv, *(T*)&t2);
+          }
+        }
+        if (lane == 0) s_alpha2 = cscale(cmulv(tk, xv), -0.5);
       }
       __syncthreads();
       const T alpha2 = s_alpha2;
