@@ -288,10 +288,10 @@ __global__ void __launch_bounds__(NT)
     if (lane == 0) ((double*)red)[warp] = ss;
     __syncthreads();  // publishes vcur (the column a, unscaled) and the warp sums
     if (warp == 0) {
-      // a butterfly over all 32 lanes (zeros beyond the warp count): every lane holds the
-      // same total, which hh_scalars_warp's lane-uniform branch and shuffles require
+      // a tree over the warps' sums (lane 0 ends with the total; hh_scalars_warp takes
+      // lane 0's operands for every lane)
       double xnorm2 = lane < nwarps ? ((double*)red)[lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) xnorm2 += __shfl_xor_sync(0xffffffffu, xnorm2, o);
+      for (int o = nwarps / 2; o > 0; o >>= 1) xnorm2 += __shfl_xor_sync(0xffffffffu, xnorm2, o);
       hh_scalars_warp(vcur[0], xnorm2, lane, s_tk, s_scale, s_beta, s_active);
       if (b == 0 && lane == 0) {
         d[k] = cre(dk);
@@ -592,10 +592,10 @@ __global__ void __launch_bounds__(kClusterTriThreads)
     // (one warp per column): with v_0 = 1, v_i = scale a_i (i > 0) and
     // alpha - beta = 1 / scale, A^H v = scale (S - beta conj(A_0,:))
     if (warp == 0) {
-      // a butterfly over all 32 lanes (zeros beyond the warp count): every lane holds the
-      // same total, which hh_scalars_warp's lane-uniform branch and shuffles require
+      // a tree over the warps' sums (lane 0 ends with the total; hh_scalars_warp takes
+      // lane 0's operands for every lane)
       double xnorm2 = lane < NW ? redd[lane] : 0.0;
-      for (int o = 16; o > 0; o >>= 1) xnorm2 += __shfl_xor_sync(0xffffffffu, xnorm2, o);
+      for (int o = NW / 2; o > 0; o >>= 1) xnorm2 += __shfl_xor_sync(0xffffffffu, xnorm2, o);
       hh_scalars_warp(vcur[0], xnorm2, lane, s_tk, s_scl, s_beta, s_active);
       if (rank == owner && lane == 0) {
         d[k] = cre(pcol[k]);
@@ -659,8 +659,8 @@ __global__ void __launch_bounds__(kClusterTriThreads)
       if (lane == 0) red[warp] = pv;
       __syncthreads();
       if (warp == 0) {
-        T xv = lane < NW ? red[lane] : czero<T>();  // a butterfly over the lanes
-        for (int o = 16; o > 0; o >>= 1) {
+        T xv = lane < NW ? red[lane] : czero<T>();  // a tree over the warps' sums (lane 0)
+        for (int o = NW / 2; o > 0; o >>= 1) {
           if constexpr (sizeof(T) == 8) {
             xv += __shfl_xor_sync(0xffffffffu, xv, o);
           } else {

@@ -16,7 +16,7 @@ struct TriEntry {
   int path;
 };
 constexpr TriEntry kTri[] = {
-    {32, 8}, {384, 16},
+    {48, 8}, {384, 16},
 };
 
 // FP64 CUDA-core GEMM: number of K slices (split K) for products whose output has
@@ -41,7 +41,7 @@ constexpr SplitEntry kSplit[] = {
     {4, 512, 32},
     {4, 1024, 32},
     {4, 2048, 32},
-    {4, 4096, 32},
+    {4, 4096, 64},
     {16, 64, 4},
     {16, 128, 8},
     {16, 256, 16},
