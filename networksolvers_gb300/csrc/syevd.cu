@@ -1632,9 +1632,8 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       if (shm) raise_smem_limit((const void*)dc_prep_kernel, shm);
       ProfScope ps(c, NSG_PROF_DC, 0.0);
       dc_prep_kernel<<<nm, 256, shm, c->stream>>>(w, Q, n, md, W);
-      dc_rotate_kernel<<<dim3((nbmax + 127) / 128, nm), 128, 0, c->stream>>>(Q, n, md, W);
     }
-    count_launch(c, 2);
+    count_launch(c);
     check_launch("dc prep");
     NSG_CUDA(cudaMemcpyAsync(cnt.data(), W.counts, sizeof(int) * 3 * nm, cudaMemcpyDeviceToHost, c->stream));
     int leaf_failed = 0;
@@ -1645,8 +1644,21 @@ static void tridiag_dc(nsg_ctx* c, int n, const std::vector<double>& d_in, const
       NSG_CHECK(leaf_failed == 0, NSG_ERR_NONFINITE, "eigensolver: a tridiagonal leaf did not converge");
       leaves_checked = true;
     }
-    int kmax = 0;
-    for (int mi = 0; mi < nm; ++mi) kmax = std::max(kmax, cnt[3 * mi]);
+    int kmax = 0, rotations = 0;
+    for (int mi = 0; mi < nm; ++mi) {
+      kmax = std::max(kmax, cnt[3 * mi]);
+      rotations += cnt[3 * mi + 1];
+    }
+    // the deflation rotations, launched only for a level that has some (the counts are
+    // on the host already for the batched product's extent)
+    if (rotations > 0) {
+      {
+        ProfScope ps(c, NSG_PROF_DC, 0.0);
+        dc_rotate_kernel<<<dim3((nbmax + 127) / 128, nm), 128, 0, c->stream>>>(Q, n, md, W);
+      }
+      count_launch(c);
+      check_launch("dc rotate");
+    }
     const int gxe = int(std::max<int64_t>(1, std::min<int64_t>(((int64_t)nbmax * nbmax + 255) / 256,
                                                                  std::max<int64_t>(1, (int64_t)c->num_sms * 8 / nm))));
     DevBuf Qm(c, sizeof(double) * (size_t)nm * nbmax * std::max(kmax, 1));
