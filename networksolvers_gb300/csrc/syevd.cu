@@ -1,10 +1,13 @@
 // Dense Hermitian eigensolver for the truncated factorizations:
-//   1. Householder reduction to a real symmetric tridiagonal T (one cooperative
-//      kernel, one grid barrier per column; the matrix stays L2-resident),
-//   2. Cuppen divide and conquer on T: implicit-QL leaves of <= 32, rank-one merges with
-//      deflation (small z / close poles), secular roots by bracketed Newton with the
-//      origin at the nearer pole (one thread per root over many CTAs), Gu-Eisenstat
-//      recomputed z for orthogonal vectors, merged by an FP64 GEMM,
+//   1. Householder reduction to a real symmetric tridiagonal T: one thread-block
+//      cluster holding the matrix in distributed shared memory (orders up to the tuning
+//      table's limit), else one cooperative kernel over all SMs with one grid barrier
+//      per column (the matrix stays L2-resident),
+//   2. Cuppen divide and conquer on T: implicit-QL leaves (8 rows by default), rank-one
+//      merges with deflation (small z / close poles), every merge of a tree level in one
+//      launch per step, secular roots by the two-pole rational model inside a bracket
+//      with the origin at the nearer pole (one warp per root), Gu-Eisenstat recomputed z
+//      for orthogonal vectors, merged by one batched product per level,
 //   3. back-transformation of the kept eigenvectors with the Householder reflectors
 //      in blocks of 64 (compact WY, three GEMMs per block; every block's T factor is
 //      formed up front in one launch).
