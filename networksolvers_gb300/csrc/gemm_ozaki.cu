@@ -191,6 +191,11 @@ struct OzEpi {
   int64_t Mp, Np;
   int a_batched, b_batched;
   int* err;
+  // split K: grid z = batch x nsplit, split s takes K slabs [s split_slabs, ..) (whole
+  // exact chunks) and writes its scaled partial product to W[z] (M x N, column-major);
+  // oz_split_reduce_kernel adds the splits in order and applies alpha and beta
+  int nsplit, split_slabs;
+  double* W;
 };
 
 // float -> double by exponent re-bias (exact for normal floats; zero, subnormals, inf and
@@ -236,8 +241,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint32_t* tmem_slot = (uint32_t*)(accempty + 1);
   volatile int* fail = (volatile int*)(tmem_slot + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN, bz = blockIdx.z;
-  const int nchunks = (nk + CHUNK_SLABS - 1) / CHUNK_SLABS;
+  const int m0 = blockIdx.x * BM, n0 = blockIdx.y * BN;
+  const int sp = int(blockIdx.z % unsigned(ep.nsplit)), bz = int(blockIdx.z / unsigned(ep.nsplit));
+  const int tb = sp * ep.split_slabs;           // this split's first K slab (global index)
+  const int nkl = min(nk - tb, ep.split_slabs);  // its slabs; the pipeline counts from 0
+  const int nchunks = (nkl + CHUNK_SLABS - 1) / CHUNK_SLABS;
 
   if (tid == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -269,11 +277,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       auto b_ptr = [&](int st, int s) { return smem + st * STAGE_BYTES + S * SLICE_A + s * SLICE_B; };
       auto issue = [&](int t, int st) {
         mbar_expect_tx(&full[st], STAGE_BYTES);
-        const int kc = t * BKS;
+        const int kc = (tb + t) * BKS;
         tma_load_3d(a_ptr(st, 0), &mapA, &full[st], kc, m0, (ep.a_batched ? bz : 0) * S);
         tma_load_3d(b_ptr(st, 0), &mapB, &full[st], kc, n0, (ep.b_batched ? bz : 0) * S);
       };
-      const int pre = nk < STAGES ? nk : STAGES;
+      const int pre = nkl < STAGES ? nkl : STAGES;
       for (int t = 0; t < pre; ++t) issue(t, t);
       int issued = pre;
       bool ok = true;
@@ -283,7 +291,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const int t0 = c * CHUNK_SLABS, t1 = min(nk, t0 + CHUNK_SLABS);
+        const int t0 = c * CHUNK_SLABS, t1 = min(nkl, t0 + CHUNK_SLABS);
         for (int t = t0; t < t1 && ok; ++t) {
           const int st = t % STAGES;
           if (!mbar_wait(&full[st], (t / STAGES) & 1, fail)) {
@@ -312,7 +320,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
           }
           mma_commit(&empty[st]);
-          if (t >= 1 && issued < nk) {
+          if (t >= 1 && issued < nkl) {
             const int sp = (t - 1) % STAGES;
             if (!mbar_wait(&empty[sp], ((t - 1) / STAGES) & 1, fail)) {
               ok = false;
@@ -395,15 +403,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (row < ep.M) {
         const int ka = pow2_exponent(ep.sa[(ep.a_batched ? bz : 0) * ep.Mp + row]);
         const bool unit_alpha = ep.alpha == 1.0;
+        double* Wz = ep.nsplit > 1 ? ep.W + (size_t)blockIdx.z * ep.M * ep.N : nullptr;
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int64_t col = n0 + 16 * q + j;
           if (col < ep.N) {
             const int kb = pow2_exponent(ep.sb[(ep.b_batched ? bz : 0) * ep.Np + col]);
             double v = scale_pow2(widen(hi[j]) + widen(lo[j]), ka + kb);
-            if (!unit_alpha) v *= ep.alpha;
-            double* cp = ep.C + bz * ep.sC + row * ep.crs + col * ep.ldc;
-            *cp = (ep.beta == 0.0) ? v : fma(ep.beta, *cp, v);
+            if (Wz) {
+              Wz[row + col * ep.M] = v;
+            } else {
+              if (!unit_alpha) v *= ep.alpha;
+              double* cp = ep.C + bz * ep.sC + row * ep.crs + col * ep.ldc;
+              *cp = (ep.beta == 0.0) ? v : fma(ep.beta, *cp, v);
+            }
           }
         }
       }
@@ -412,6 +425,21 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
   if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(512));
+}
+
+// C = alpha sum_s W[b nsplit + s] + beta C, the splits added in order
+__global__ void oz_split_reduce_kernel(const double* __restrict__ W, int nsplit, int64_t M, int64_t N,
+                                       int64_t batch, double* __restrict__ C, int64_t ldc, int64_t sC, int64_t crs,
+                                       double alpha, double beta) {
+  const int64_t MN = M * N, tot = MN * batch;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < tot; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t b = e / MN, r = e - b * MN, row = r % M, col = r / M;
+    double acc = 0.0;
+    for (int sp = 0; sp < nsplit; ++sp) acc += W[(b * nsplit + sp) * MN + r];
+    const double v = alpha == 1.0 ? acc : acc * alpha;
+    double* cp = C + b * sC + row * crs + col * ldc;
+    *cp = (beta == 0.0) ? v : fma(beta, *cp, v);
+  }
 }
 
 using EncodeFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
@@ -500,13 +528,46 @@ void oz_product(nsg_ctx* c, const OzOperand& A, const OzOperand& B, int64_t M, i
               mB = make_map(B.slices, B.rows_p, K_p, S * B.batch, BN, S);
   int* err = device_flag(c);  // checked once at the end of the public call
   ensure_smem_limit((const void*)oz_gemm_kernel<S>, SMEM_BYTES);
-  OzEpi ep{C, ldc, sC, M, N, crs, alpha, beta, A.scales, B.scales, A.rows_p, B.rows_p, A.batch > 1, B.batch > 1, err};
-  dim3 grid(unsigned(A.rows_p / BM), unsigned(B.rows_p / BN), unsigned(batch));
+  // split K over whole exact chunks when the output tiles would leave most SMs idle
+  // (the small products of a converged sweep: 32-64 tiles of 128 x 64 on 152 SMs)
+  const int nk = int(K_p / BKS), nchunk = (nk + CHUNK_SLABS - 1) / CHUNK_SLABS;
+  const int64_t tiles = (A.rows_p / BM) * (B.rows_p / BN) * batch;
+  const int64_t sms = c->num_sms > 0 ? c->num_sms : 152;
+  int nsplit = 1;
+  if (tiles * 2 <= sms && nchunk >= 2)
+    nsplit = int(std::min<int64_t>({(int64_t)nchunk, sms / tiles, 16, 65535 / batch}));
+  const int split_slabs = (nchunk + nsplit - 1) / nsplit * CHUNK_SLABS;
+  nsplit = (nk + split_slabs - 1) / split_slabs;
+  // the partial products' workspace, only when K is split (freed on every exit)
+  struct Partials {
+    nsg_ctx* c;
+    void* p;
+    size_t bytes;
+    ~Partials() {
+      try {
+        dfree(c, p, bytes);
+      } catch (...) {
+      }
+    }
+  } wbuf{c, nullptr, 0};
+  if (nsplit > 1) {
+    wbuf.bytes = sizeof(double) * size_t(nsplit) * size_t(batch) * size_t(M) * size_t(N);
+    wbuf.p = dalloc(c, wbuf.bytes);
+  }
+  OzEpi ep{C,        ldc,         sC,          M,     N,     crs,  alpha, beta, A.scales, B.scales, A.rows_p, B.rows_p,
+           A.batch > 1, B.batch > 1, err, nsplit, split_slabs, (double*)wbuf.p};
+  dim3 grid(unsigned(A.rows_p / BM), unsigned(B.rows_p / BN), unsigned(batch * nsplit));
   {
     ProfScope ps(c, NSG_PROF_TC_GEMM, 2.0 * double(M) * double(N) * double(flop_k) * double(batch));
-    oz_gemm_kernel<S><<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, int(K_p / BKS), ep);
+    oz_gemm_kernel<S><<<grid, NTHREADS, SMEM_BYTES, c->stream>>>(mA, mB, nk, ep);
+    if (nsplit > 1) {
+      const int64_t tot = M * N * batch;
+      const int rg = int(std::min<int64_t>((tot + 255) / 256, sms * 8));
+      oz_split_reduce_kernel<<<rg, 256, 0, c->stream>>>((const double*)wbuf.p, nsplit, M, N, batch, C, ldc, sC, crs,
+                                                        alpha, beta);
+    }
   }
-  count_launch(c);
+  count_launch(c, nsplit > 1 ? 2 : 1);
   check_launch("oz_gemm");
 }
 

@@ -130,3 +130,28 @@ def test_complex_ozaki_gemm(nsg_ctx, precision, bound):
             nsg_ctx.set_precision("fp64")
         assert prof["tc_gemm"]["launches"] == 4, prof
         assert np.max(np.abs(c - ref) / scale) < bound, (ia, ib, ca, cb)
+
+
+@pytest.mark.parametrize("precision,bound", [("ozaki", 1e-13), ("ozaki8", 1e-15)])
+@pytest.mark.parametrize("m,k,n", [(100, 3000, 70), (300, 1000, 200)])
+def test_ozaki_split_k_small_outputs(nsg_ctx, precision, bound, m, k, n):
+    """Products whose 128 x 64 output tiles would leave most SMs idle split K over whole
+    exact chunks (up to 16 splits; the partial products added in order, then alpha and
+    beta): the same bound relative to the row and column scales as one pass over K."""
+    rng = np.random.default_rng(m + k + n)
+    i, j, l = Index(m), Index(n), Index(k)
+    a = rng.standard_normal((m, k))
+    a[:, 1] *= 1e4
+    b = rng.standard_normal((k, n))
+    ref = a @ b
+    A, B = DTensor.from_numpy(a, (i, l)), DTensor.from_numpy(b, (l, j))
+    nsg_ctx.set_precision(precision)
+    try:
+        before = nsg_ctx.counters()["launches"]
+        c = contract([A, B], out=[i, j]).to_numpy()
+        launches = nsg_ctx.counters()["launches"] - before
+    finally:
+        nsg_ctx.set_precision("fp64")
+    scale = np.abs(a).max(axis=1)[:, None] * np.abs(b).max(axis=0)[None, :] * k
+    assert np.max(np.abs(c - ref) / scale) < bound
+    assert launches >= 6  # two operands sliced (2 launches each), the product and its split reduction
