@@ -16,8 +16,9 @@ tridiagonalisation, the secular equations and the Lanczos scalars stay FP64;
 (`--workload c1|tdvp|batch|serve|accuracy|qn`) print their own lines; see `main()`.
 
 Timing: CUDA events on the library's stream around each timed sweep; the per-kernel
-roofline comes from events around each launch of the dominant kernel classes in the
-same region.  Inputs larger than L2: the two-site tensors, environments and GEMM
+roofline and the kernel shares come from events around each launch of the kernel
+classes in one further sweep after the timed ones (nothing is recorded inside the timed
+sweeps).  Inputs larger than L2: the two-site tensors, environments and GEMM
 operands at bond dimension >= 512 are 8-170 MB each and are rewritten every region.
 """
 from __future__ import annotations
