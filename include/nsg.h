@@ -102,6 +102,25 @@ int nsg_ctx_event_elapsed(nsg_ctx* ctx, int slot_from, int slot_to, float* ms);
 int nsg_ctx_profile(nsg_ctx* ctx, int enable);
 int nsg_ctx_profile_read(nsg_ctx* ctx, int cls, uint64_t* launches, double* ms, double* flops);
 
+/* Per-phase timers of the region step (the reference's timed examples wrap each plugin
+ * in @elapsed; here the device time on the context's stream).  While enabled
+ * (nsg_ctx_timers), the host brackets the phases of a region step with
+ * nsg_ctx_phase(ctx, phase, 1) ... nsg_ctx_phase(ctx, phase, 0), which record CUDA events
+ * on the context's stream, and the library brackets every linear-map application
+ * (NSG_PHASE_HEFF) and the phases of nsg_region_step itself.  nsg_get_timers synchronises
+ * and returns per phase the number of closed intervals and their summed device
+ * milliseconds (arrays of NSG_PHASE_NCOUNT).  Phases may nest (H_eff inside Krylov, the
+ * expansion inside extraction); a phase may not be opened twice.  Enabling resets. */
+#define NSG_PHASE_EXTRACT 0   /* gauge walk, region product, environment updates  */
+#define NSG_PHASE_SUBSPACE 1  /* density-matrix subspace expansion                */
+#define NSG_PHASE_KRYLOV 2    /* local solver: eigsolve / exponentiate / Runge-Kutta */
+#define NSG_PHASE_HEFF 3      /* linear-map (H_eff) applications                  */
+#define NSG_PHASE_FACTORIZE 4 /* truncated factorization of the inserter          */
+#define NSG_PHASE_NCOUNT 5
+int nsg_ctx_timers(nsg_ctx* ctx, int enable);
+int nsg_ctx_phase(nsg_ctx* ctx, int phase, int begin);
+int nsg_get_timers(nsg_ctx* ctx, uint64_t* counts, double* ms);
+
 /* Diagnostic of the timeout path (no counterpart in the reference): launches a kernel
  * that waits on the context's stream, with the bounded pattern of the library's own
  * device waits, for a device flag that nothing sets.  After `polls` polls (1..2^24, each

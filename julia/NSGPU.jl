@@ -61,6 +61,30 @@ set_precision!(c::Ctx, p::Symbol) = check(c, @ccall lib.nsg_ctx_set_precision(c.
 const TUNING = Dict(:splitk => 0, :tridiag => 1, :dc_leaf => 2)
 set_tuning!(c::Ctx, p::Symbol, v::Integer) =
   check(c, @ccall lib.nsg_ctx_set_tuning(c.h::Ptr{Cvoid}, TUNING[p]::Cint, Cint(v)::Cint)::Cint)
+# per-phase device timers of the region step: the overrides below bracket their phases,
+# the library brackets every H_eff application itself
+const PHASES = (:extract, :subspace, :krylov, :heff, :factorize)
+const TIMING = Ref(false)  # whether the overrides bracket their phases
+function timers!(c::Ctx, on::Bool)
+  check(c, @ccall lib.nsg_ctx_timers(c.h::Ptr{Cvoid}, Cint(on)::Cint)::Cint)
+  TIMING[] = on
+  return nothing
+end
+function phase(f, c::Ctx, p::Symbol)
+  TIMING[] || return f()
+  k = Cint(findfirst(==(p), PHASES) - 1)
+  check(c, @ccall lib.nsg_ctx_phase(c.h::Ptr{Cvoid}, k::Cint, Cint(1)::Cint)::Cint)
+  try
+    return f()
+  finally
+    check(c, @ccall lib.nsg_ctx_phase(c.h::Ptr{Cvoid}, k::Cint, Cint(0)::Cint)::Cint)
+  end
+end
+function timers(c::Ctx)
+  n = zeros(UInt64, length(PHASES)); ms = zeros(Float64, length(PHASES))
+  check(c, @ccall lib.nsg_get_timers(c.h::Ptr{Cvoid}, n::Ptr{UInt64}, ms::Ptr{Float64})::Cint)
+  return Dict(p => (count=n[i], ms=ms[i]) for (i, p) in enumerate(PHASES))
+end
 
 # ---------------------------------------------------------------------------
 # device tensors: an ITensor's dense storage is column-major in index order, the

@@ -53,6 +53,9 @@ _SIGS = {
     "nsg_ctx_profile_read": (i32, [p, i32, C.POINTER(u64), P_dbl, P_dbl]),
     "nsg_ctx_wait_probe": (i32, [p, i64]),
     "nsg_ctx_set_tuning": (i32, [p, i32, i32]),
+    "nsg_ctx_timers": (i32, [p, i32]),
+    "nsg_ctx_phase": (i32, [p, i32, i32]),
+    "nsg_get_timers": (i32, [p, C.POINTER(u64), P_dbl]),
     "nsg_tensor_create": (i32, [p, i32, i32, P_i64, P_p]),
     "nsg_tensor_upload": (i32, [p, i32, i32, P_i64, p, P_p]),
     "nsg_tensor_download": (i32, [p, p, p]),
@@ -107,11 +110,16 @@ def exported_symbols():
     return list(_SIGS)
 
 
+# the region step's phases, in the order of NSG_PHASE_* (include/nsg.h)
+PHASES = ["extract", "subspace", "krylov", "heff", "factorize"]
+
+
 class Context:
     """Owns an nsg_ctx (one CUDA stream + memory pool on one device)."""
 
     def __init__(self, device=0, hbm_budget=0, precision="fp64"):
         self.L = lib()
+        self.timing = False
         h = C.c_void_p()
         self._check_raw(self.L.nsg_ctx_create(device, hbm_budget, C.byref(h)), None)
         self.h = h
@@ -171,6 +179,24 @@ class Context:
             out[nm] = dict(launches=n.value, ms=ms.value, flops=fl.value)
         return out
 
+    def timers(self, enable):
+        """Per-phase device timers of the region step (nsg_ctx_timers); enabling resets."""
+        self.check(self.L.nsg_ctx_timers(self.h, int(enable)))
+        self.timing = bool(enable)
+
+    def phase(self, name, begin):
+        """Open (begin=True) or close a phase interval on the context's stream; a no-op
+        unless the timers run."""
+        if self.timing:
+            self.check(self.L.nsg_ctx_phase(self.h, PHASES.index(name), int(bool(begin))))
+
+    def read_timers(self):
+        """{phase: {"count": closed intervals, "ms": summed device milliseconds}}."""
+        n = (u64 * len(PHASES))()
+        ms = (dbl * len(PHASES))()
+        self.check(self.L.nsg_get_timers(self.h, n, ms))
+        return {nm: dict(count=n[k], ms=ms[k]) for k, nm in enumerate(PHASES)}
+
     def close(self):
         if getattr(self, "h", None):
             self.L.nsg_ctx_destroy(self.h)
@@ -197,6 +223,12 @@ def default_context():
     if _default is None:
         _default = Context()
     return _default
+
+
+def current_context():
+    """The context default_context() would return, or None when none exists yet (creates
+    nothing)."""
+    return getattr(_local, "ctx", None) or _default
 
 
 def set_default_context(ctx):

@@ -577,6 +577,7 @@ int nsg_linmap_apply(nsg_ctx* c, nsg_linmap* m, const nsg_tensor* x, nsg_tensor*
   NSG_CHECK(x->rank == int(m->x_labels.size()) && y->size == x->size && x->dtype == y->dtype &&
                 (m->n_fixed == 0 || x->dtype == m->dtype),
             NSG_ERR_INVALID, "linmap_apply: x/y shape or dtype mismatch");
+  PhaseScope phase(c, NSG_PHASE_HEFF);
   LT xl;
   xl.t = const_cast<nsg_tensor*>(x);
   xl.lab = m->x_labels;

@@ -211,11 +211,24 @@ static void clear_profile(nsg_ctx* c) {
   c->prof.clear();
 }
 
+static void clear_phases(nsg_ctx* c) {
+  for (auto& r : c->phases) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  c->phases.clear();
+  for (auto& e : c->phase_open) {
+    if (e) cudaEventDestroy(e);
+    e = nullptr;
+  }
+}
+
 int nsg_ctx_destroy(nsg_ctx* c) {
   if (!c) return NSG_OK;
   cudaSetDevice(c->device);
   cudaStreamSynchronize(c->stream);
   clear_profile(c);
+  clear_phases(c);
   for (auto& e : c->events)
     if (e) cudaEventDestroy(e);
   if (c->host_scalars) cudaFreeHost(c->host_scalars);
@@ -285,6 +298,53 @@ int nsg_ctx_profile_read(nsg_ctx* c, int cls, uint64_t* launches, double* ms, do
   if (launches) *launches = n;
   if (ms) *ms = t;
   if (flops) *flops = f;
+  NSG_API_END(c)
+}
+
+int nsg_ctx_timers(nsg_ctx* c, int enable) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c, NSG_ERR_INVALID, "null context");
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  clear_phases(c);
+  c->timing = enable != 0;
+  NSG_API_END(c)
+}
+
+int nsg_ctx_phase(nsg_ctx* c, int phase, int begin) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && phase >= 0 && phase < NSG_PHASE_NCOUNT, NSG_ERR_INVALID, "phase out of range");
+  if (c->timing) {
+    cudaEvent_t& open = c->phase_open[phase];
+    if (begin) {
+      NSG_CHECK(open == nullptr, NSG_ERR_INVALID, "phase already open");
+      NSG_CUDA(cudaEventCreate(&open));
+      NSG_CUDA(cudaEventRecord(open, c->stream));
+    } else {
+      NSG_CHECK(open != nullptr, NSG_ERR_INVALID, "phase not open");
+      cudaEvent_t b = nullptr;
+      NSG_CUDA(cudaEventCreate(&b));
+      NSG_CUDA(cudaEventRecord(b, c->stream));
+      c->phases.push_back({phase, open, b, 0.0});
+      open = nullptr;
+    }
+  }
+  NSG_API_END(c)
+}
+
+int nsg_get_timers(nsg_ctx* c, uint64_t* counts, double* ms) {
+  NSG_API_BEGIN(c)
+  NSG_CHECK(c && counts && ms, NSG_ERR_INVALID, "null argument");
+  NSG_CUDA(cudaStreamSynchronize(c->stream));
+  for (int p = 0; p < NSG_PHASE_NCOUNT; ++p) {
+    counts[p] = 0;
+    ms[p] = 0.0;
+  }
+  for (auto& r : c->phases) {
+    float e = 0;
+    NSG_CUDA(cudaEventElapsedTime(&e, r.a, r.b));
+    counts[r.cls] += 1;
+    ms[r.cls] += e;
+  }
   NSG_API_END(c)
 }
 

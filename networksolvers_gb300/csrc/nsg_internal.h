@@ -78,6 +78,9 @@ struct nsg_ctx {
     double flops;
   };
   std::vector<ProfRec> prof;
+  bool timing = false;                           // per-phase timers (nsg_ctx_timers)
+  cudaEvent_t phase_open[NSG_PHASE_NCOUNT] = {};  // start event of each open phase
+  std::vector<ProfRec> phases;                   // closed intervals (cls = phase)
 };
 
 namespace nsg {
@@ -131,6 +134,26 @@ struct ProfScope {
     if (a) {
       cudaEventRecord(b, c->stream);
       c->prof.push_back({cls, a, b, flops});
+    }
+  }
+};
+// Brackets a phase of the region step with CUDA events while the context's timers run.
+struct PhaseScope {
+  nsg_ctx* c;
+  int phase;
+  cudaEvent_t a = nullptr;
+  PhaseScope(nsg_ctx* cc, int p) : c(cc), phase(p) {
+    if (c->timing) {
+      cudaEventCreate(&a);
+      cudaEventRecord(a, c->stream);
+    }
+  }
+  ~PhaseScope() {
+    if (a) {
+      cudaEvent_t b = nullptr;
+      cudaEventCreate(&b);
+      cudaEventRecord(b, c->stream);
+      c->phases.push_back({phase, a, b, 0.0});
     }
   }
 };

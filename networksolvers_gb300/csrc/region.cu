@@ -27,6 +27,7 @@ int nsg_region_step(nsg_ctx* c, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, n
   // product psi1 [a, s1, c] psi2 [c, s2, b] -> local [a, s1, s2, b]
   nsg_tensor* local = nullptr;
   {
+    PhaseScope phase(c, NSG_PHASE_EXTRACT);
     nsg_tensor* ts[2] = {const_cast<nsg_tensor*>(psi1), const_cast<nsg_tensor*>(psi2)};
     const int32_t labs[6] = {a, s1, cb, cb, s2, b};
     const int32_t outl[4] = {a, s1, s2, b};
@@ -46,7 +47,11 @@ int nsg_region_step(nsg_ctx* c, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, n
     }
   }
   int numops = 0;
-  int rc = nsg_eigsolve(c, m, local, krylovdim, maxiter, tol, energy, &numops);
+  int rc;
+  {
+    PhaseScope phase(c, NSG_PHASE_KRYLOV);
+    rc = nsg_eigsolve(c, m, local, krylovdim, maxiter, tol, energy, &numops);
+  }
   nsg_linmap_release(c, m);
   if (rc != NSG_OK) {
     nsg_tensor_release(c, local);
@@ -58,8 +63,11 @@ int nsg_region_step(nsg_ctx* c, nsg_tensor* L, nsg_tensor* W1, nsg_tensor* W2, n
   // C [k, a, s1] -> left site as [a, s1, k].
   const int axes0[2] = {0, 1}, axes1[2] = {2, 3};
   nsg_tensor *U = nullptr, *Cf = nullptr;
-  rc = nsg_factorize(c, local, direction == 0 ? axes0 : axes1, 2, cutoff, maxdim, mindim, &U, &Cf, newdim, truncerr,
-                     nullptr, 0);
+  {
+    PhaseScope phase(c, NSG_PHASE_FACTORIZE);
+    rc = nsg_factorize(c, local, direction == 0 ? axes0 : axes1, 2, cutoff, maxdim, mindim, &U, &Cf, newdim,
+                       truncerr, nullptr, 0);
+  }
   nsg_tensor_release(c, local);
   NSG_CHECK(rc == NSG_OK, rc, std::string("region_step: ") + c->err);
   if (direction == 0) {

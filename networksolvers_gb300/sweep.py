@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+from contextlib import contextmanager
 
 import numpy as np
 
@@ -184,7 +185,8 @@ def subspace_expand(problem, local, region_iterator, algorithm, trunc, expansion
     prec = ctx.precision
     ctx.set_precision("ozaki8" if prec in ("ozaki", "ozaki8") else "fp64")
     try:
-        return _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass, perp)
+        with _phase("subspace"):
+            return _densitymatrix(problem, local, region, P, psi, pv, nv, A, Cn, a, tr, north_pass, perp)
     finally:
         ctx.set_precision(prec)
 
@@ -316,11 +318,29 @@ def region_step(L, W1, W2, R, psi1, psi2, direction=0, krylovdim=3, maxiter=1, t
 # ----------------------------------------------------------------------------
 
 
+@contextmanager
+def _phase(name):
+    """Brackets a phase of the region step on the current context's stream while its
+    per-phase timers run (Context.timers); nothing otherwise."""
+    ctx = N.current_context()
+    timing = ctx is not None and ctx.timing
+    if timing:
+        ctx.phase(name, True)
+    try:
+        yield
+    finally:
+        if timing:
+            ctx.phase(name, False)
+
+
 def region_iterator_action(problem, region_iterator, updater, extracter_kwargs=None, updater_kwargs=None,
                            inserter_kwargs=None, sweep=1, **kws):
-    problem, local = extracter(problem, region_iterator, **{**dict(extracter_kwargs or {}), "sweep": sweep, **kws})
-    problem, local = updater(problem, local, region_iterator, **{**dict(updater_kwargs or {}), **kws})
-    problem = inserter(problem, local, region_iterator, **{"sweep": sweep, **dict(inserter_kwargs or {}), **kws})
+    with _phase("extract"):
+        problem, local = extracter(problem, region_iterator, **{**dict(extracter_kwargs or {}), "sweep": sweep, **kws})
+    with _phase("krylov"):
+        problem, local = updater(problem, local, region_iterator, **{**dict(updater_kwargs or {}), **kws})
+    with _phase("factorize"):
+        problem = inserter(problem, local, region_iterator, **{"sweep": sweep, **dict(inserter_kwargs or {}), **kws})
     return problem
 
 
