@@ -49,3 +49,13 @@ def test_committed_table_parses_and_matches_json():
         d = json.loads(js.read_text())
         assert [tuple(x) for x in d["table"]["tridiag"]] == tri
         assert [tuple(x) for x in d["table"]["splitk"]] == split
+
+
+def test_rewrite_tables_from_saved_measurements(tmp_path):
+    # the committed measurements rewrite to the committed header (no GPU needed)
+    js = PKG / "tuning.json"
+    if not js.exists():
+        return
+    assert at.main(["--from-json", str(js), "--out", str(tmp_path)]) == 0
+    assert parse_header((tmp_path / "tuning_table.h").read_text()) == parse_header(
+        (PKG / "csrc" / "tuning_table.h").read_text())
