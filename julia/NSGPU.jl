@@ -362,21 +362,24 @@ end
 
 # extracter.jl:3-17
 function ns.extracter(problem::Union{DevEig,DevExp}, region_iterator; sweep, trunc=(;), kws...)
-  trunc = ns.truncation_parameters(sweep; trunc...)
-  region = ns.current_region(region_iterator)
-  psi = orthogonalize(ns.state(problem), region)
-  local_state = length(region) == 1 ? psi[only(region)] : contract(psi.ctx, [psi[v] for v in region])
-  problem = setproperties(problem; state=psi)
-  problem, local_state = ns.subspace_expand(problem, local_state, region_iterator; sweep, trunc, kws...)
-  P = ns.operator(problem)
-  position!(P, ns.state(problem), region)
-  return setproperties(problem; operator=P), local_state
+  return phase(ns.state(problem).ctx, :extract) do
+    trunc = ns.truncation_parameters(sweep; trunc...)
+    region = ns.current_region(region_iterator)
+    psi = orthogonalize(ns.state(problem), region)
+    local_state = length(region) == 1 ? psi[only(region)] : contract(psi.ctx, [psi[v] for v in region])
+    problem = setproperties(problem; state=psi)
+    problem, local_state = ns.subspace_expand(problem, local_state, region_iterator; sweep, trunc, kws...)
+    P = ns.operator(problem)
+    position!(P, ns.state(problem), region)
+    return setproperties(problem; operator=P), local_state
+  end
 end
 
 # subspace/densitymatrix.jl:5-74 on the device
 function ns.subspace_expand(::ns.Backend"densitymatrix", problem::Union{DevEig,DevExp}, local_state::DT,
                             region_iterator; north_pass=1, expansion_factor=ns.default_expansion_factor(),
                             max_expand=ns.default_max_expand(), trunc, kws...)
+  return phase(ns.state(problem).ctx, :subspace) do
   region = ns.current_region(region_iterator)
   psi = copy(ns.state(problem))
   P = ns.operator(problem)
@@ -421,21 +424,26 @@ function ns.subspace_expand(::ns.Backend"densitymatrix", problem::Union{DevEig,D
   psi[nv] = contract(psi.ctx, [expander, C])
   local_state = contract(psi.ctx, [expander, local_state])
   return setproperties(problem; state=psi), local_state
+  end  # phase
 end
 
 # eigsolve.jl:14-28
 function ns.updater(E::DevEig, local_state::DT, region_iterator; outputlevel, solver=eigsolve_solver, kws...)
   P = ns.operator(E)
-  m = LinMap(P.ctx, map_tensors(P), local_state.inds)
-  eigval, local_state = solver(m, local_state; kws...)
-  return setproperties(E; eigenvalue=eigval), local_state
+  return phase(P.ctx, :krylov) do
+    m = LinMap(P.ctx, map_tensors(P), local_state.inds)
+    eigval, x = solver(m, local_state; kws...)
+    return setproperties(E; eigenvalue=eigval), x
+  end
 end
 
 # applyexp.jl:18-48 (the 1-site bond back-evolution included)
 function ns.updater(T::DevExp, local_state::DT, region_iterator; nsites, time_step, solver=runge_kutta_solver,
                     outputlevel, kws...)
   P = ns.operator(T)
-  local_state, _ = solver(LinMap(P.ctx, map_tensors(P), local_state.inds), time_step, local_state; kws...)
+  local_state = phase(P.ctx, :krylov) do
+    first(solver(LinMap(P.ctx, map_tensors(P), local_state.inds), time_step, local_state; kws...))
+  end
   if nsites == 1
     curr, nxt = ns.current_region(region_iterator), ns.next_region(region_iterator)
     if !isnothing(nxt) && nxt != curr
@@ -456,6 +464,7 @@ end
 # inserter.jl:3-33
 function ns.inserter(problem::Union{DevEig,DevExp}, local_tensor::DT, region_iterator; normalize=false,
                      set_orthogonal_region=true, sweep, trunc=(;), kws...)
+  return phase(ns.state(problem).ctx, :factorize) do
   trunc = ns.truncation_parameters(sweep; trunc...)
   region = ns.current_region(region_iterator)
   psi = copy(ns.state(problem))
@@ -472,6 +481,7 @@ function ns.inserter(problem::Union{DevEig,DevExp}, local_tensor::DT, region_ite
   set_orthogonal_region && (psi.ortho_region = [v])
   normalize && scale!(psi[v], 1 / norm(psi[v]))
   return setproperties(problem; state=psi)
+  end  # phase
 end
 
 ns.state(ψ::DeviceTTN) = ψ
